@@ -1,0 +1,344 @@
+"""Benchmark: 30-qubit depth-40 f64 circuit on one GB300 (zeno's state-vector hot path).
+
+Workload: u3(theta, phi, lambda) with U[0, 2pi) angles on every qubit, then CX
+on a seeded random perfect matching, 40 layers, 30 qubits, f64 split-complex
+state (16 GiB, far larger than L2, so no flush is needed between steps),
+measure all, 1024 shots. One step = one circuit: reset to |0...0>, every
+compiled op, then sampling.
+
+Prints ONE JSON line (rank 0). `value` = circuits/s with the op stream
+resident on the device side of the API; `e2e` = the same through
+`zc_run` (state allocation, op tables host->device, kernels, sampling,
+indices device->host). `roofline` = the dominant kernel's algorithmic HBM
+bytes per launch over its CUDA-event duration; `cpu_baseline` = the oracle
+(the C restatement of zeno's CPU backend) on all host cores for a bounded
+sample of the same workload.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+HBM_FALLBACK_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--qubits", type=int, default=30)
+    ap.add_argument("--depth", type=int, default=40)
+    ap.add_argument("--precision", type=int, default=64)
+    ap.add_argument("--fusion", type=int, default=1)
+    ap.add_argument("--mode", default="exact", choices=["exact", "fast"])
+    ap.add_argument("--shots", type=int, default=1024)
+    ap.add_argument("--seed", type=int, default=7)
+    ap.add_argument("--cpu-layers", type=int, default=1, help="layers timed for the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return HBM_FALLBACK_GBS, "fallback"
+
+
+def workload_name(a):
+    return "%dq depth-%d u3+matching-CX f%d, %d shots, fusion %d, %s arithmetic" % (
+        a.qubits, a.depth, a.precision, a.shots, a.fusion, a.mode)
+
+
+class Clocks:
+    """nvidia-smi clock / throttle sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, dev):
+        self.dev = dev
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        rows = []
+        try:
+            for line in open(self.path):
+                f = [x.strip() for x in line.split(",")]
+                if len(f) >= 9:
+                    rows.append(f)
+        except Exception:
+            pass
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def op_class(op, zc):
+    if op.kind == zc.OP_UNITARY:
+        return "1q" if len(op.qubits) == 1 else "kq%d" % len(op.qubits)
+    if op.kind == zc.OP_DIAG:
+        return "diag"
+    if op.kind == zc.OP_CX:
+        return "cx"
+    if op.kind == zc.OP_SWAP:
+        return "swap"
+    return "other"
+
+
+def op_bytes(op, zc, state_bytes):
+    """Algorithmic HBM bytes of one op: a full pass reads and writes the state
+    (2S); CX / SWAP move only the half that changes (S)."""
+    return state_bytes if op.kind in (zc.OP_CX, zc.OP_SWAP) else 2 * state_bytes
+
+
+def cpu_baseline(a, threads=None):
+    """The oracle on the host cores for a bounded sample: state allocation,
+    `cpu_layers` layers of the circuit and the sampler, scaled to one circuit."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    from zeno_gb300 import circuit as C
+
+    oracle.build()
+    oracle.set_threads(threads or os.cpu_count() or 1)
+    nthreads = oracle.threads()
+    layer = C.matching_circuit(a.qubits, a.cpu_layers, a.seed, measure=False).to_program()
+    comp = oracle.compile(layer, a.fusion)
+    t0 = time.perf_counter()
+    st = oracle.State(a.qubits, a.precision)
+    t1 = time.perf_counter()
+    for op in comp.ops:
+        st.apply_op(op)
+    t2 = time.perf_counter()
+    st.sample(a.shots, 1)
+    t3 = time.perf_counter()
+    st.close()
+    per_circuit = (t1 - t0) + (t2 - t1) * a.depth / a.cpu_layers + (t3 - t2)
+    return {
+        "value": 1.0 / per_circuit, "unit": "circuits/s", "cores": nthreads, "kind": "port",
+        "sample": "%d of %d layers (%d ops) + state allocation + %d-shot sampling on %d threads, "
+                  "layer time scaled x%d" % (a.cpu_layers, a.depth, len(comp.ops), a.shots, nthreads,
+                                              a.depth // a.cpu_layers),
+        "seconds_sampled": t3 - t0,
+    }
+
+
+def dist_init(a):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0
+    import torch.distributed as dist
+
+    rank = int(os.environ["RANK"])
+    local = int(os.environ.get("LOCAL_RANK", rank))
+    import torch
+
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        dist.init_process_group("gloo")
+    return rank, ws, local
+
+
+def reference_arm(a):
+    rank, ws, _ = dist_init(a)
+    if rank != 0:
+        return
+    steps = []
+    for i in range(a.warmup + a.steps):
+        r = cpu_baseline(a)
+        if i >= a.warmup:
+            steps.append(r)
+    v = statistics.median(s["value"] for s in steps)
+    line = {
+        "impl": "reference", "metric": "30q circuit throughput (u3 + matching-CX, depth 40, f64)",
+        "value": v, "unit": "circuits/s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if a.precision == 64 else "f32", "data": "synthetic (seeded circuit)",
+        "config": {"workload": workload_name(a), "l2": "state 16 GiB > L2, no flush needed"},
+        "cpu_baseline": {k: steps[-1][k] for k in ("kind", "cores", "sample")} | {"value": v,
+                                                                                 "unit": "circuits/s"},
+        "e2e": {"value": v, "unit": "circuits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "C restatement of zeno's scalar CPU backend (the Rust binary cannot be built here)",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        return reference_arm(a)
+    rank, ws, local = dist_init(a)
+    import torch
+
+    from zeno_gb300 import backend as zc
+    from zeno_gb300 import build as zb
+    from zeno_gb300 import circuit as C
+    from zeno_gb300.rng import splitmix64
+
+    if rank == 0:
+        zb.build()
+    if ws > 1:
+        torch.distributed.barrier()
+    zc.load()
+    dev = local
+    torch.cuda.set_device(dev)
+    flags = zc.FLAG_FAST if a.mode == "fast" else zc.FLAG_EXACT
+    circ = C.matching_circuit(a.qubits, a.depth, a.seed).to_program()
+    prog = zc.compile(circ, a.fusion)
+    ops = prog.ops
+    be = zc.CudaBackend(a.qubits, a.precision, flags)
+    stream = torch.cuda.ExternalStream(be.stream())
+    S = (1 << a.qubits) * (a.precision // 8) * 2
+    sample_seed = splitmix64(a.seed)
+
+    def step(events=None):
+        be.reset_all()
+        if events is not None:
+            events[0].record(stream)
+        for i, op in enumerate(ops):
+            if op.kind == zc.OP_UNITARY:
+                be.apply_unitary(op.qubits, op.data)
+            elif op.kind == zc.OP_DIAG:
+                be.apply_diagonal(op.qubits, op.data)
+            elif op.kind == zc.OP_CX:
+                be.apply_cx(op.a, op.b)
+            elif op.kind == zc.OP_SWAP:
+                be.apply_swap(op.a, op.b)
+            if events is not None:
+                events[i + 1].record(stream)
+        return be.sample(a.shots, sample_seed)
+
+    for _ in range(a.warmup):
+        step()
+    be.finish()
+    c0 = be.counters()
+    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(len(ops) + 1)] for _ in range(a.steps)]
+    if ws > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with Clocks(dev) as clk:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        t_start.record(stream)
+        for k in range(a.steps):
+            step(evs[k])
+        t_end.record(stream)
+        be.finish()
+        torch.cuda.synchronize()
+    if ws > 1:
+        torch.distributed.barrier()
+    elapsed = t_start.elapsed_time(t_end) / 1000.0
+    c1 = be.counters()
+    if ws > 1:
+        t = torch.tensor([elapsed], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        elapsed = float(t.item())
+    # per-kernel-class durations from the per-op events
+    classes = {}
+    for k in range(a.steps):
+        for i, op in enumerate(ops):
+            c = op_class(op, zc)
+            ms = evs[k][i].elapsed_time(evs[k][i + 1])
+            d = classes.setdefault(c, {"launches": 0, "ms": 0.0, "bytes": 0})
+            d["launches"] += 1
+            d["ms"] += ms
+            d["bytes"] += op_bytes(op, zc, S)
+    gates_ms = sum(d["ms"] for d in classes.values())
+    dom = max(classes, key=lambda c: classes[c]["ms"])
+    dd = classes[dom]
+    peak, peak_kind = peaks()
+    achieved = (dd["bytes"] / dd["launches"]) / (dd["ms"] / dd["launches"] / 1000.0) / 1e9
+    value = a.steps * ws / elapsed
+    line = {
+        "metric": "30q circuit throughput (u3 + matching-CX, depth 40, f64)",
+        "value": value, "unit": "circuits/s", "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": elapsed / a.steps * 1000.0, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if a.precision == 64 else "f32",
+        "data": "synthetic (seeded circuit, random angles)",
+        "config": {"workload": workload_name(a), "parallelism": "replicas" if ws > 1 else "single",
+                   "l2": "state %.0f GiB > 129 MB L2: no flush needed" % (S / 2**30),
+                   "ops": len(ops), "input_gates": prog.stats["input_gates"]},
+        "gpu_launches": int(c1["launches"] - c0["launches"]),
+        "kernels": {c: {"launches": d["launches"], "avg_ms": d["ms"] / d["launches"],
+                        "GBps": (d["bytes"] / d["launches"]) / (d["ms"] / d["launches"] / 1000.0) / 1e9,
+                        "share": d["ms"] / gates_ms} for c, d in sorted(classes.items())},
+        "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "bytes_per_launch": dd["bytes"] / dd["launches"], "traffic": None},
+        "clocks": clk.summary(),
+    }
+    if not a.no_e2e:
+        torch.cuda.synchronize()
+        be.close()
+        h2d = 0
+        for op in ops:
+            if op.kind in (zc.OP_UNITARY, zc.OP_DIAG):
+                h2d += op.data.size * 2 * (a.precision // 8)
+        h2d += a.shots * 8
+        d2h = a.shots * 8 + max(1, (1 << a.qubits) >> 16) * 8
+        zc.run(circ, shots=a.shots, seed=a.seed, precision=a.precision, flags=flags, program=prog)
+        ts = []
+        for _ in range(max(1, min(a.steps, 2))):
+            t0 = time.perf_counter()
+            r = zc.run(circ, shots=a.shots, seed=a.seed, precision=a.precision, flags=flags, program=prog)
+            ts.append(time.perf_counter() - t0)
+        line["e2e"] = {"value": 1.0 / statistics.median(ts), "unit": "circuits/s", "h2d_bytes_per_step": h2d,
+                       "d2h_bytes_per_step": d2h, "sim_seconds": r.sim_time,
+                       "path": "zc_run: allocate state, per-op host->device tables, kernels, sample, read indices"}
+    if rank == 0 and not a.no_cpu:
+        line["cpu_baseline"] = cpu_baseline(a)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -879,7 +879,7 @@ struct zo_state {
 static int g_threads = 0;
 void zo_set_threads(int t) {
     g_threads = t;
-    if (t > 0) omp_set_num_threads(t);
+    omp_set_num_threads(t > 0 ? t : omp_get_num_procs());
 }
 int zo_get_threads(void) { return g_threads > 0 ? g_threads : omp_get_max_threads(); }
 

@@ -1,0 +1,62 @@
+"""The C-ABI library loads, exports every entry point the header declares,
+and refuses cleanly where no GPU is present. CPU only."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    src = open(os.path.join(ROOT, "include", "zeno_cuda.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(zc_[a-z0-9_]+)\s*\(", src)))
+
+
+def test_header_exports(zc):
+    lib = ctypes.CDLL(zc.LIB_PATH)
+    names = declared_symbols()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert sorted(zc.EXPORTS) == names
+
+
+def test_capacity_planning(zc):
+    """mem.rs retargeted to HBM: 33 qubits f64 / 34 f32 in 0.75 x 284208 MiB."""
+    hbm = 284208 * (1 << 20)
+    budget = int(hbm * 0.75)
+    assert zc.max_qubits(budget, 64) == 33
+    assert zc.max_qubits(budget, 32) == 34
+    assert zc.state_bytes(30, 64) == 16 << 30
+    assert zc.max_qubits(24 << 30, 64) == 30 and zc.max_qubits(24 << 30, 32) == 31
+
+
+def test_env_budget_override(zc, monkeypatch):
+    monkeypatch.setenv("ZENO_MEM_BYTES", str(16 << 30))
+    assert zc.device_budget() == 16 << 30
+
+
+def _have_gpu():
+    try:
+        import torch
+
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_have_gpu(), reason="checks the no-GPU refusal path")
+def test_create_without_gpu_fails_loudly(zc):
+    with pytest.raises(zc.ZenoCudaError) as e:
+        zc.CudaBackend(4, 64)
+    assert e.value.code in (zc.ZC_ERR_UNSUPPORTED, zc.ZC_ERR_CUDA)
+
+
+def test_invalid_arguments_rejected_before_device(zc, monkeypatch):
+    monkeypatch.setenv("ZENO_MEM_BYTES", str(1 << 20))
+    with pytest.raises(zc.ZenoCudaError):
+        zc.CudaBackend(4, 48)  # bad precision

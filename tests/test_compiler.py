@@ -1,0 +1,89 @@
+"""The backend's host compiler (libzeno_cuda zc_compile) against the oracle's
+restatement of compiler::compile (src/compiler.rs:118-626): same op kinds,
+supports and bit-identical fused matrices at every fusion level 0..6.
+Runs on CPU (the compiler needs no GPU)."""
+
+import math
+
+import numpy as np
+import pytest
+
+import refmats
+from helpers import program_from_json
+from test_oracle import _mixed
+from zeno_gb300 import circuit as C
+
+pytestmark = []
+
+
+def _same_ops(zc, oracle, p, fusion):
+    mine = zc.compile(p, fusion, swap_perm=False)
+    ref = oracle.compile(p, fusion)
+    assert mine.dynamic == ref.dynamic
+    assert mine.final_measures == ref.final_measures
+    assert mine.stats == ref.stats
+    a, b = mine.ops, ref.ops
+    assert len(a) == len(b)
+    for x, y in zip(a, b):
+        assert x.kind == y.kind
+        if x.kind in (0, 1):
+            assert x.qubits == y.qubits
+            assert np.array_equal(x.data.view(np.float64), y.data.view(np.float64))
+        elif x.kind == 2:
+            assert (x.a, x.b) == (y.control, y.target)
+        elif x.kind in (3, 4):
+            assert x.a == y.qubit
+        assert x.cond == y.cond
+
+
+@pytest.mark.parametrize("n", [2, 3, 5, 8])
+def test_compiler_matches_oracle(zc, oracle, n):
+    for c in (C.random_circuit(n, 12, 100 + n), _mixed(n, 80, 700 + n), C.matching_circuit(n, 6, 5)):
+        for fusion in range(7):
+            _same_ops(zc, oracle, c.to_program(), fusion)
+
+
+def test_compiler_examples(zc, oracle, examples):
+    for name, d in examples.items():
+        p = program_from_json(d)
+        for fusion in (0, 1, 5):
+            _same_ops(zc, oracle, p, fusion)
+
+
+def test_swap_stays_a_permutation(zc):
+    c = C.Circuit(4)
+    c.h(0).swap(3, 1).measure_all()
+    ops = zc.compile(c.to_program(), 1).ops
+    assert [o.kind for o in ops] == [0, 6]
+    assert (ops[1].a, ops[1].b) == (1, 3)
+
+
+def test_fusion7_support(zc):
+    c = C.Circuit(8)
+    for q in range(7):
+        c.h(q)
+    for q in range(6):
+        c.cx(q, q + 1)
+    p = zc.compile(c.to_program(), 7)
+    assert p.stats["max_fused"] == 7 and len(p.ops) == 1
+    u = p.ops[0].data.reshape(128, 128)
+    assert np.abs(u @ u.conj().T - np.eye(128)).max() < 1e-12
+
+
+def test_compile_errors(zc):
+    c = C.Circuit(2)
+    c.gate("cx", [0, 0])
+    with pytest.raises(zc.ZenoCudaError, match="duplicate"):
+        zc.compile(c.to_program())
+    c = C.Circuit(2)
+    c.gate("foo", [0])
+    with pytest.raises(zc.ZenoCudaError, match="unknown gate"):
+        zc.compile(c.to_program())
+    c = C.Circuit(2)
+    c.gate("rx", [0], [])
+    with pytest.raises(zc.ZenoCudaError, match="parameter"):
+        zc.compile(c.to_program())
+    c = C.Circuit(2)
+    c.gate("h", [5])
+    with pytest.raises(zc.ZenoCudaError, match="out of range"):
+        zc.compile(c.to_program())

@@ -1,0 +1,416 @@
+// C ABI of the backend (include/zeno_cuda.h): state lifecycle, argument
+// validation, op dispatch onto the gate kernels, reductions, the sampler's
+// host half, and HBM capacity planning.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <string>
+#include <vector>
+
+#include "zc_internal.h"
+#include "zc_rng.h"
+
+namespace zc {
+
+static thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char *where) {
+    g_err = std::string("CUDA error in ") + where + ": " + cudaGetErrorString(e);
+    return ZC_ERR_CUDA;
+}
+
+static std::string human_bytes(double b) {
+    const char *units[] = {"B", "KiB", "MiB", "GiB", "TiB"};
+    int u = 0;
+    while (b >= 1024.0 && u < 4) {
+        b /= 1024.0;
+        u++;
+    }
+    char buf[64];
+    if (u == 0)
+        snprintf(buf, sizeof buf, "%.0f B", b);
+    else
+        snprintf(buf, sizeof buf, "%.1f %s", b, units[u]);
+    return buf;
+}
+
+static constexpr size_t kArenaBytes = 32u << 20;
+
+// Copy `bytes` into the device parameter ring and return its device address.
+static int arena_put(zc_state *st, const void *src, size_t bytes, const void **dev) {
+    Arena &a = st->arena;
+    const size_t need = (bytes + 255) & ~(size_t)255;
+    if (need > a.cap) return fail(ZC_ERR_INVALID, "op table larger than the parameter arena");
+    if (a.head + need > a.cap) {
+        ZC_CUDA(cudaStreamSynchronize(st->stream));
+        a.head = 0;
+    }
+    memcpy(a.host + a.head, src, bytes);
+    ZC_CUDA(cudaMemcpyAsync(a.dev + a.head, a.host + a.head, bytes, cudaMemcpyHostToDevice, st->stream));
+    *dev = a.dev + a.head;
+    a.head += need;
+    return ZC_OK;
+}
+
+// Stage a complex table (interleaved c64) as split T arrays [re..., im...].
+static int stage_table(zc_state *st, const double *c64, size_t count, const void **dev) {
+    if (st->prec == 64) {
+        std::vector<double> t(2 * count);
+        for (size_t i = 0; i < count; i++) {
+            t[i] = c64[2 * i];
+            t[count + i] = c64[2 * i + 1];
+        }
+        return arena_put(st, t.data(), t.size() * sizeof(double), dev);
+    }
+    std::vector<float> t(2 * count);
+    for (size_t i = 0; i < count; i++) {
+        t[i] = (float)c64[2 * i];
+        t[count + i] = (float)c64[2 * i + 1];
+    }
+    return arena_put(st, t.data(), t.size() * sizeof(float), dev);
+}
+
+static int check_support(const zc_state *st, const uint32_t *qs, uint32_t k, uint32_t kmax, const char *what) {
+    if (!st) return fail(ZC_ERR_INVALID, "null state");
+    if (k < 1 || k > kmax) return fail(ZC_ERR_INVALID, std::string(what) + ": support size out of range");
+    if (!qs) return fail(ZC_ERR_INVALID, std::string(what) + ": null qubit list");
+    for (uint32_t i = 0; i < k; i++) {
+        if (qs[i] >= st->n) return fail(ZC_ERR_INVALID, std::string(what) + ": qubit out of range");
+        if (i && qs[i] <= qs[i - 1])
+            return fail(ZC_ERR_INVALID, std::string(what) + ": qubits must be sorted and distinct");
+    }
+    return ZC_OK;
+}
+
+static inline bool exact(const zc_state *st) { return (st->flags & ZC_FLAG_FAST) == 0; }
+
+static int sync_read_scalar(zc_state *st, double *out) {
+    ZC_CUDA(cudaMemcpyAsync(st->h_scalar, st->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, st->stream));
+    ZC_CUDA(cudaStreamSynchronize(st->stream));
+    *out = *st->h_scalar;
+    return ZC_OK;
+}
+
+static int grow(void **p, size_t *cap, size_t need) {
+    if (need <= *cap) return ZC_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    ZC_CUDA(cudaMalloc(p, need));
+    *cap = need;
+    return ZC_OK;
+}
+
+}  // namespace zc
+
+using namespace zc;
+
+extern "C" {
+
+const char *zc_last_error(void) { return g_err.c_str(); }
+
+uint64_t zc_state_bytes(uint32_t n, int prec) { return (n >= 64 ? 0 : (1ull << n)) * (prec == 32 ? 8u : 16u); }
+
+uint32_t zc_max_qubits(uint64_t budget, int prec) {
+    uint32_t n = 0;
+    while ((((unsigned __int128)1) << (n + 1)) * (unsigned __int128)(prec == 32 ? 8 : 16) <= budget) {
+        n++;
+        if (n >= 60) break;
+    }
+    return n;
+}
+
+int zc_device_budget(double fraction, uint64_t *bytes) {
+    if (!bytes) return fail(ZC_ERR_INVALID, "null output");
+    const char *env = getenv("ZENO_MEM_BYTES");
+    if (env && *env) {
+        char *end = nullptr;
+        unsigned long long v = strtoull(env, &end, 10);
+        if (end && *end == 0) {
+            *bytes = v;
+            return ZC_OK;
+        }
+    }
+    size_t free_b = 0, total_b = 0;
+    cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemGetInfo");
+    *bytes = (uint64_t)((double)total_b * fraction);
+    return ZC_OK;
+}
+
+int zc_create(uint32_t n, int prec, zc_state **out) { return zc_create_ex(n, prec, ZC_FLAG_EXACT, out); }
+
+int zc_create_ex(uint32_t n, int prec, uint32_t flags, zc_state **out) {
+    if (!out) return fail(ZC_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    if (prec != 32 && prec != 64) return fail(ZC_ERR_INVALID, "precision_bits must be 32 or 64");
+    if (n < 1 || n > 48) return fail(ZC_ERR_INVALID, "qubit count must be in 1..=48");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(ZC_ERR_UNSUPPORTED, std::string("no usable CUDA device: ") + cudaGetErrorString(e));
+    uint64_t budget = 0;
+    int rc = zc_device_budget(0.75, &budget);
+    if (rc) return rc;
+    const uint64_t need = zc_state_bytes(n, prec);
+    if (need > budget) {
+        char buf[256];
+        snprintf(buf, sizeof buf,
+                 "state vector for %u qubits at f%d needs %s but the budget is %s (max %u qubits at this "
+                 "precision; raise --mem-limit or lower qubits)",
+                 n, prec, human_bytes((double)need).c_str(), human_bytes((double)budget).c_str(),
+                 zc_max_qubits(budget, prec));
+        return fail(ZC_ERR_MEMORY, buf);
+    }
+    zc_state *st = new zc_state();
+    st->n = n;
+    st->prec = prec;
+    st->flags = flags;
+    st->device = dev;
+    st->len = 1ull << n;
+    st->name = prec == 64 ? "cuda-f64" : "cuda-f32";
+    cudaDeviceGetAttribute(&st->num_sms, cudaDevAttrMultiProcessorCount, dev);
+    if (st->num_sms <= 0) st->num_sms = 1;
+    const size_t bytes = st->len * (prec / 8);
+#define TRY(call)                          \
+    do {                                   \
+        cudaError_t e_ = (call);           \
+        if (e_ != cudaSuccess) {           \
+            int r_ = cuda_fail(e_, #call); \
+            zc_destroy(st);                \
+            return r_;                     \
+        }                                  \
+    } while (0)
+    TRY(cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking));
+    e = cudaMalloc(&st->re, bytes);
+    if (e == cudaSuccess) e = cudaMalloc(&st->im, bytes);
+    if (e != cudaSuccess) {
+        fail(ZC_ERR_MEMORY, std::string("device allocation of the state failed: ") + cudaGetErrorString(e));
+        cudaGetLastError();
+        zc_destroy(st);
+        return ZC_ERR_MEMORY;
+    }
+    TRY(cudaMallocHost(&st->arena.host, kArenaBytes));
+    TRY(cudaMalloc(&st->arena.dev, kArenaBytes));
+    st->arena.cap = kArenaBytes;
+    TRY(cudaMalloc(&st->d_scalar, sizeof(double)));
+    TRY(cudaMallocHost(&st->h_scalar, sizeof(double)));
+#undef TRY
+    rc = launch_reset(st);
+    if (rc) {
+        zc_destroy(st);
+        return rc;
+    }
+    *out = st;
+    return ZC_OK;
+}
+
+void zc_destroy(zc_state *st) {
+    if (!st) return;
+    if (st->stream) cudaStreamSynchronize(st->stream);
+    if (st->re) cudaFree(st->re);
+    if (st->im) cudaFree(st->im);
+    if (st->arena.host) cudaFreeHost(st->arena.host);
+    if (st->arena.dev) cudaFree(st->arena.dev);
+    if (st->d_part) cudaFree(st->d_part);
+    if (st->d_scalar) cudaFree(st->d_scalar);
+    if (st->h_scalar) cudaFreeHost(st->h_scalar);
+    if (st->d_samp) cudaFree(st->d_samp);
+    if (st->stream) cudaStreamDestroy(st->stream);
+    delete st;
+}
+
+const char *zc_name(const zc_state *st) { return st ? st->name.c_str() : ""; }
+
+int zc_apply_unitary(zc_state *st, const uint32_t *qs, uint32_t k, const double *mat) {
+    int rc = check_support(st, qs, k, kMaxUnitaryQubits, "apply_unitary");
+    if (rc) return rc;
+    if (!mat) return fail(ZC_ERR_INVALID, "apply_unitary: null matrix");
+    st->ctr.ops++;
+    if (k == 1) return launch_1q(st, qs[0], mat, exact(st));
+    const void *dev = nullptr;
+    rc = stage_table(st, mat, (size_t)1 << (2 * k), &dev);
+    if (rc) return rc;
+    return launch_kq(st, qs, k, dev, exact(st));
+}
+
+int zc_apply_diagonal(zc_state *st, const uint32_t *qs, uint32_t k, const double *d) {
+    int rc = check_support(st, qs, k, kMaxDiagQubits, "apply_diagonal");
+    if (rc) return rc;
+    if (!d) return fail(ZC_ERR_INVALID, "apply_diagonal: null diagonal");
+    st->ctr.ops++;
+    if (k == 1) return launch_diag1(st, qs[0], d, exact(st));
+    const void *dev = nullptr;
+    rc = stage_table(st, d, (size_t)1 << k, &dev);
+    if (rc) return rc;
+    return launch_diagk(st, qs, k, dev, exact(st));
+}
+
+int zc_apply_cx(zc_state *st, uint32_t c, uint32_t t) {
+    if (!st) return fail(ZC_ERR_INVALID, "null state");
+    if (c >= st->n || t >= st->n || c == t) return fail(ZC_ERR_INVALID, "apply_cx: bad control/target");
+    if (st->n < 2) return fail(ZC_ERR_INVALID, "apply_cx: needs two qubits");
+    st->ctr.ops++;
+    return launch_cx(st, c, t);
+}
+
+int zc_apply_swap(zc_state *st, uint32_t a, uint32_t b) {
+    if (!st) return fail(ZC_ERR_INVALID, "null state");
+    if (a >= st->n || b >= st->n || a == b) return fail(ZC_ERR_INVALID, "apply_swap: bad qubits");
+    st->ctr.ops++;
+    return launch_swap(st, a, b);
+}
+
+int zc_prob_one(zc_state *st, uint32_t q, double *out) {
+    if (!st || !out) return fail(ZC_ERR_INVALID, "null argument");
+    if (q >= st->n) return fail(ZC_ERR_INVALID, "prob_one: qubit out of range");
+    size_t nch = 0;
+    int rc = launch_chunk_sums(st, 1, q, &nch);
+    if (rc) return rc;
+    rc = launch_serial_sum(st, nch);
+    if (rc) return rc;
+    return sync_read_scalar(st, out);
+}
+
+int zc_measure(zc_state *st, uint32_t q, double u, int *outcome) {
+    if (!outcome) return fail(ZC_ERR_INVALID, "null argument");
+    double p1 = 0.0;
+    int rc = zc_prob_one(st, q, &p1);
+    if (rc) return rc;
+    const int o = u < p1;
+    const double p = o ? p1 : 1.0 - p1;
+    rc = launch_collapse(st, q, o, 1.0 / sqrt(p));
+    if (rc) return rc;
+    *outcome = o;
+    return ZC_OK;
+}
+
+int zc_reset_all(zc_state *st) {
+    if (!st) return fail(ZC_ERR_INVALID, "null state");
+    return launch_reset(st);
+}
+
+int zc_norm_sqr(zc_state *st, double *out) {
+    if (!st || !out) return fail(ZC_ERR_INVALID, "null argument");
+    size_t nch = 0;
+    int rc = launch_chunk_sums(st, 0, 0, &nch);
+    if (rc) return rc;
+    rc = launch_serial_sum(st, nch);
+    if (rc) return rc;
+    return sync_read_scalar(st, out);
+}
+
+// Backend::sample: pass 1 (chunk masses) and pass 2 (per-chunk rescans) run
+// on the GPU; the serial prefix, the serial draws, the sort and the routing
+// (src/sample.rs:51-62) run on the host, exactly as the reference orders them.
+int zc_sample(zc_state *st, uint64_t shots, uint64_t seed, uint64_t *out) {
+    if (!st) return fail(ZC_ERR_INVALID, "null state");
+    if (shots == 0) return ZC_OK;
+    if (!out) return fail(ZC_ERR_INVALID, "sample: null output");
+    size_t nch = 0;
+    int rc = launch_chunk_sums(st, 0, 0, &nch);
+    if (rc) return rc;
+    std::vector<double> sums(nch);
+    ZC_CUDA(cudaMemcpyAsync(sums.data(), st->d_part, nch * sizeof(double), cudaMemcpyDeviceToHost, st->stream));
+    ZC_CUDA(cudaStreamSynchronize(st->stream));
+    std::vector<double> cum(nch + 1);
+    cum[0] = 0.0;
+    for (size_t c = 0; c < nch; c++) cum[c + 1] = cum[c] + sums[c];
+    const double total = cum[nch];
+    Xoshiro rng(seed);
+    std::vector<double> us(shots);
+    for (uint64_t i = 0; i < shots; i++) us[i] = rng.f64() * total;
+    std::sort(us.begin(), us.end());
+    std::vector<SampleChunk> touched;
+    size_t prev = std::lower_bound(us.begin(), us.end(), cum[0]) - us.begin();
+    for (size_t c = 0; c < nch; c++) {
+        const size_t next = std::lower_bound(us.begin(), us.end(), cum[c + 1]) - us.begin();
+        if (prev < next) touched.push_back(SampleChunk{c, prev, next, cum[c]});
+        prev = next;
+    }
+    const uint64_t chunk_len = st->len < (1ull << kSampleChunkLog2) ? st->len : (1ull << kSampleChunkLog2);
+    const size_t us_b = shots * sizeof(double), out_b = shots * sizeof(uint64_t);
+    const size_t cs_b = touched.size() * sizeof(SampleChunk);
+    rc = grow(&st->d_samp, &st->samp_cap, us_b + out_b + cs_b + 64);
+    if (rc) return rc;
+    char *base = (char *)st->d_samp;
+    double *d_us = (double *)base;
+    uint64_t *d_out = (uint64_t *)(base + us_b);
+    SampleChunk *d_cs = (SampleChunk *)(base + us_b + out_b);
+    ZC_CUDA(cudaMemcpyAsync(d_us, us.data(), us_b, cudaMemcpyHostToDevice, st->stream));
+    ZC_CUDA(cudaMemsetAsync(d_out, 0, out_b, st->stream));
+    if (!touched.empty())
+        ZC_CUDA(cudaMemcpyAsync(d_cs, touched.data(), cs_b, cudaMemcpyHostToDevice, st->stream));
+    rc = launch_sample_scan(st, d_cs, touched.size(), d_us, d_out, chunk_len);
+    if (rc) return rc;
+    ZC_CUDA(cudaMemcpyAsync(out, d_out, out_b, cudaMemcpyDeviceToHost, st->stream));
+    ZC_CUDA(cudaStreamSynchronize(st->stream));
+    return ZC_OK;
+}
+
+int zc_statevector(zc_state *st, double *out) {
+    if (!st || !out) return fail(ZC_ERR_INVALID, "null argument");
+    const size_t es = st->prec / 8;
+    std::vector<char> re(st->len * es), im(st->len * es);
+    ZC_CUDA(cudaMemcpyAsync(re.data(), st->re, st->len * es, cudaMemcpyDeviceToHost, st->stream));
+    ZC_CUDA(cudaMemcpyAsync(im.data(), st->im, st->len * es, cudaMemcpyDeviceToHost, st->stream));
+    ZC_CUDA(cudaStreamSynchronize(st->stream));
+    for (size_t i = 0; i < st->len; i++) {
+        if (st->prec == 64) {
+            out[2 * i] = ((double *)re.data())[i];
+            out[2 * i + 1] = ((double *)im.data())[i];
+        } else {
+            out[2 * i] = (double)((float *)re.data())[i];
+            out[2 * i + 1] = (double)((float *)im.data())[i];
+        }
+    }
+    return ZC_OK;
+}
+
+int zc_load_state(zc_state *st, const double *in) {
+    if (!st || !in) return fail(ZC_ERR_INVALID, "null argument");
+    const size_t es = st->prec / 8;
+    std::vector<char> re(st->len * es), im(st->len * es);
+    for (size_t i = 0; i < st->len; i++) {
+        if (st->prec == 64) {
+            ((double *)re.data())[i] = in[2 * i];
+            ((double *)im.data())[i] = in[2 * i + 1];
+        } else {
+            ((float *)re.data())[i] = (float)in[2 * i];
+            ((float *)im.data())[i] = (float)in[2 * i + 1];
+        }
+    }
+    ZC_CUDA(cudaMemcpyAsync(st->re, re.data(), st->len * es, cudaMemcpyHostToDevice, st->stream));
+    ZC_CUDA(cudaMemcpyAsync(st->im, im.data(), st->len * es, cudaMemcpyHostToDevice, st->stream));
+    ZC_CUDA(cudaStreamSynchronize(st->stream));
+    return ZC_OK;
+}
+
+int zc_finish(zc_state *st) {
+    if (!st) return fail(ZC_ERR_INVALID, "null state");
+    ZC_CUDA(cudaStreamSynchronize(st->stream));
+    ZC_CUDA(cudaGetLastError());
+    return ZC_OK;
+}
+
+int zc_get_stream(zc_state *st, void **stream) {
+    if (!st || !stream) return fail(ZC_ERR_INVALID, "null argument");
+    *stream = (void *)st->stream;
+    return ZC_OK;
+}
+
+int zc_get_counters(zc_state *st, zc_counters *out) {
+    if (!st || !out) return fail(ZC_ERR_INVALID, "null argument");
+    *out = st->ctr;
+    return ZC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,94 @@
+// Internal declarations shared by the CUDA translation units of libzeno_cuda.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/zeno_cuda.h"
+
+namespace zc {
+
+// Sets the thread-local error text and returns `code`.
+int fail(int code, const std::string &msg);
+int cuda_fail(cudaError_t e, const char *where);
+
+#define ZC_CUDA(call)                                   \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) return zc::cuda_fail(e_, #call); \
+    } while (0)
+
+constexpr int kMaxUnitaryQubits = 7;
+constexpr int kMaxDiagQubits = 12;
+constexpr int kSampleChunkLog2 = 16;  // sample.rs CHUNK = 1 << 16
+
+// Device parameter arena: tables (matrices, diagonals) for queued ops are
+// staged in pinned host memory and copied into a device ring. Wrapping the
+// ring synchronises the stream, so no slot is reused while in flight.
+struct Arena {
+    char *host = nullptr;
+    char *dev = nullptr;
+    size_t cap = 0;
+    size_t head = 0;
+};
+
+struct Launch {
+    int blocks;
+    int threads;
+};
+
+}  // namespace zc
+
+struct zc_state {
+    uint32_t n = 0;
+    int prec = 64;  // 32 or 64
+    uint32_t flags = 0;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    void *re = nullptr;  // device, 2^n elements of T
+    void *im = nullptr;
+    size_t len = 0;
+    zc::Arena arena;
+    // scratch for reductions and the sampler
+    double *d_part = nullptr;  // chunk partial sums
+    size_t part_cap = 0;
+    double *d_scalar = nullptr;  // single result
+    double *h_scalar = nullptr;  // pinned
+    void *d_samp = nullptr;      // sampler work area
+    size_t samp_cap = 0;
+    zc_counters ctr{};
+    std::string name;
+};
+
+namespace zc {
+
+// Kernel launchers (zc_gates.cu / zc_reduce.cu). All are asynchronous on
+// st->stream and return ZC_OK or an error code.
+int launch_1q(zc_state *st, uint32_t q, const double *m8, bool exact);
+int launch_kq(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat, bool exact);
+int launch_diag1(zc_state *st, uint32_t q, const double *d4, bool exact);
+int launch_diagk(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_diag, bool exact);
+int launch_cx(zc_state *st, uint32_t c, uint32_t t);
+int launch_swap(zc_state *st, uint32_t a, uint32_t b);
+int launch_reset(zc_state *st);
+int launch_collapse(zc_state *st, uint32_t q, int outcome, double scale64);
+// f64 partial sums of |amp|^2 over chunks of 2^16 (serial within a chunk).
+// mode 0: all amplitudes (norm / sampler pass 1); mode 1: the q=1 half of
+// qubit q (prob_one). Writes nchunks partials to st->d_part.
+int launch_chunk_sums(zc_state *st, int mode, uint32_t q, size_t *nchunks);
+// Serial in-order sum of st->d_part[0..nchunks) into st->d_scalar.
+int launch_serial_sum(zc_state *st, size_t nchunks);
+// Sampler pass 2 (sample.rs:64-108): one thread per touched chunk.
+struct SampleChunk {
+    uint64_t chunk;  // chunk index
+    uint64_t s0, s1; // draw range
+    double cum;      // cum_before[chunk]
+};
+int launch_sample_scan(zc_state *st, const SampleChunk *d_chunks, size_t nchunks, const double *d_us,
+                       uint64_t *d_out, uint64_t chunk_len);
+
+}  // namespace zc

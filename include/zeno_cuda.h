@@ -33,6 +33,7 @@ extern "C" {
 #define ZC_FLAG_EXACT 0u      /* reference arithmetic, no FMA: bit-exact with zeno's CPU kernels */
 #define ZC_FLAG_FAST 1u       /* FMA-contracted arithmetic (tolerance parity, not bit-exact) */
 #define ZC_FLAG_NO_SWEEPS 2u  /* one launch per op: disables multi-op sweep scheduling */
+#define ZC_FLAG_FORCE_SWEEPS 4u /* schedule sweeps even for small states (testing) */
 
 typedef struct zc_state zc_state;
 

@@ -1,0 +1,154 @@
+"""Multi-op sweeps and the fast arithmetic modes.
+
+Exact mode: a sweep applies its ops in program order (permutations may move
+past disjoint ops, which is exact), so the state must stay bit-identical to
+the oracle applying the same ops one by one. Fast mode (FMA for f32,
+double-float on the FP32 pipe for f64) must stay within 1e-12 (f64) and
+1e-5 (f32) of the exact oracle.
+"""
+
+import numpy as np
+import pytest
+
+from helpers import bits_equal, rand_matrix, rand_state
+from zeno_gb300 import circuit as C
+
+pytestmark = pytest.mark.gpu
+
+
+def replay(zc, oracle, n, prec, ops, flags, amps=None):
+    g = zc.CudaBackend(n, prec, flags)
+    o = oracle.State(n, prec)
+    if amps is not None:
+        g.load_state(amps)
+        o.load(amps)
+    for op in ops:
+        kind = op[0]
+        if kind == "u":
+            g.apply_unitary(op[1], op[2])
+            o.apply_unitary(op[1], op[2])
+        elif kind == "d":
+            g.apply_diagonal(op[1], op[2])
+            o.apply_diagonal(op[1], op[2])
+        elif kind == "cx":
+            g.apply_cx(op[1], op[2])
+            o.apply_cx(op[1], op[2])
+        elif kind == "swap":
+            swap = np.zeros((4, 4), complex)
+            for c in range(4):
+                swap[((c & 1) << 1) | ((c >> 1) & 1), c] = 1
+            g.apply_swap(op[1], op[2])
+            o.apply_unitary(sorted(op[1:3]), swap)
+    return g, o
+
+
+def random_ops(n, count, seed, with_kq=True):
+    rng = np.random.default_rng(seed)
+    ops = []
+    for i in range(count):
+        r = rng.integers(0, 10)
+        if r < 4:
+            q = int(rng.integers(0, n))
+            ops.append(("u", [q], rand_matrix(2, seed * 1000 + i)))
+        elif r < 5:
+            k = int(rng.integers(1, 5))
+            qs = sorted(int(x) for x in rng.choice(n, k, replace=False))
+            ops.append(("d", qs, rand_state(k, seed * 1000 + i)))
+        elif r < 7:
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            ops.append(("cx", a, b))
+        elif r < 8:
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            ops.append(("swap", a, b))
+        elif with_kq and r < 9:
+            qs = sorted(int(x) for x in rng.choice(n, 2, replace=False))
+            ops.append(("u", qs, rand_matrix(4, seed * 1000 + i)))
+        else:
+            q = int(rng.integers(0, n))
+            ops.append(("d", [q], rand_state(1, i)))
+    return ops
+
+
+@pytest.mark.parametrize("prec", (64, 32))
+@pytest.mark.parametrize("n", (4, 7, 11, 14, 17))
+def test_forced_sweeps_bit_exact(zc, oracle, prec, n):
+    amps = rand_state(n, n, normalize=True)
+    ops = random_ops(n, 160, 10 + n)
+    g, o = replay(zc, oracle, n, prec, ops, zc.FLAG_FORCE_SWEEPS, amps)
+    a, b = g.statevector(), o.statevector()
+    assert bits_equal(a, b), "max |d| = %g" % np.abs(a - b).max()
+    c = g.counters()
+    assert c["launches"] < len(ops), c  # ops were batched
+    g.close()
+
+
+@pytest.mark.parametrize("prec", (64, 32))
+def test_default_sweeps_20q_circuit(zc, oracle, prec):
+    p = C.matching_circuit(20, 12, 7).to_program()
+    r = zc.run(p, shots=2048, seed=7, precision=prec, statevector=True)
+    ref, _, sv, _ = oracle.run(p, prec=prec, shots=2048, seed=7, statevector=True)
+    assert bits_equal(r.statevector, sv)
+    assert r.counts == ref
+    assert r.sweeps < 12 * 30, r.sweeps  # far fewer passes than ops
+
+
+def test_sweeps_with_reads_between(zc, oracle):
+    """Flush points (prob_one, measure, norm) must see every queued op."""
+    n = 16
+    amps = rand_state(n, 3, normalize=True)
+    ops = random_ops(n, 60, 99, with_kq=False)
+    g, o = replay(zc, oracle, n, 64, ops[:30], zc.FLAG_EXACT, amps)
+    assert g.prob_one(5) == o.prob_one(5)
+    assert g.measure(9, 0.4) == o.measure(9, 0.4)
+    for op in ops[30:]:
+        if op[0] == "u":
+            g.apply_unitary(op[1], op[2]); o.apply_unitary(op[1], op[2])
+        elif op[0] == "d":
+            g.apply_diagonal(op[1], op[2]); o.apply_diagonal(op[1], op[2])
+        elif op[0] == "cx":
+            g.apply_cx(op[1], op[2]); o.apply_cx(op[1], op[2])
+    assert g.norm_sqr() == o.norm_sqr()
+    assert bits_equal(g.statevector(), o.statevector())
+    g.close()
+
+
+@pytest.mark.parametrize("n", (6, 15, 20))
+def test_fast_mode_f64_within_1e12(zc, oracle, n):
+    amps = rand_state(n, 5, normalize=True)
+    ops = [op for op in random_ops(n, 200, 40 + n) if not (op[0] == "u" and len(op[1]) > 1)]
+    # unitary matrices for realistic magnitudes
+    ops = [("u", op[1], np.linalg.qr(op[2])[0]) if op[0] == "u" else op for op in ops]
+    ops = [("d", op[1], op[2] / np.abs(op[2])) if op[0] == "d" else op for op in ops]
+    for flags in (zc.FLAG_FAST, zc.FLAG_FAST | zc.FLAG_FORCE_SWEEPS, zc.FLAG_FAST | zc.FLAG_NO_SWEEPS):
+        g, o = replay(zc, oracle, n, 64, ops, flags, amps)
+        d = np.abs(g.statevector() - o.statevector()).max()
+        assert d < 1e-12, (flags, d)
+        g.close()
+
+
+def test_fast_mode_f32_within_1e5(zc, oracle):
+    n = 18
+    p = C.matching_circuit(n, 10, 3).to_program()
+    exact = oracle.run(p, prec=64, shots=0, statevector=True)[2]
+    r = zc.run(p, shots=0, precision=32, statevector=True, flags=zc.FLAG_FAST)
+    assert np.abs(r.statevector - exact).max() < 1e-5
+
+
+@pytest.mark.parametrize("n", (20, 24))
+def test_fast_mode_circuit_vs_fp64_oracle(zc, oracle, n):
+    """max|d amp| <= 1e-12 and TVD <= 1e-6 against the FP64 oracle."""
+    p = C.matching_circuit(n, 12, 11).to_program()
+    _, _, sv, _ = oracle.run(p, prec=64, shots=0, statevector=True)
+    r = zc.run(p, shots=0, precision=64, statevector=True, flags=zc.FLAG_FAST)
+    d = np.abs(r.statevector - sv).max()
+    tvd = 0.5 * np.abs(np.abs(r.statevector) ** 2 - np.abs(sv) ** 2).sum()
+    assert d < 1e-12 and tvd < 1e-6, (d, tvd)
+
+
+def test_fast_mode_qft_with_swaps(zc, oracle):
+    c, x = C.qft_circuit(16, 5)
+    p = c.to_program()
+    r = zc.run(p, shots=4096, seed=2, precision=64, statevector=True, flags=zc.FLAG_FAST)
+    dim = 1 << 16
+    want = np.exp(2j * np.pi * x * np.arange(dim) / dim) / np.sqrt(dim)
+    assert np.abs(r.statevector - want).max() < 1e-12

@@ -13,6 +13,7 @@
 
 #include "zc_internal.h"
 #include "zc_rng.h"
+#include "zc_sweep.h"
 
 namespace zc {
 
@@ -110,6 +111,237 @@ static int grow(void **p, size_t *cap, size_t need) {
     return ZC_OK;
 }
 
+
+// ------------------------------------------------------------------ scheduling
+
+static constexpr size_t kQueueWindow = 2048;  // ops examined per sweep plan
+static constexpr size_t kQueueFlushAt = 8192; // queue length that forces a flush
+static constexpr uint32_t kMinSweepQubits = 14;
+
+static int launch_single(zc_state *st, const QOp &op) {
+    const bool ex = exact(st);
+    switch (op.kind) {
+        case Q_UNITARY: {
+            if (op.k == 1) return launch_1q(st, op.qs[0], op.data.data(), ex);
+            const void *dev = nullptr;
+            int rc = stage_table(st, op.data.data(), (size_t)1 << (2 * op.k), &dev);
+            if (rc) return rc;
+            return launch_kq(st, op.qs, op.k, dev, ex);
+        }
+        case Q_DIAG: {
+            if (op.k == 1) return launch_diag1(st, op.qs[0], op.data.data(), ex);
+            const void *dev = nullptr;
+            int rc = stage_table(st, op.data.data(), (size_t)1 << op.k, &dev);
+            if (rc) return rc;
+            return launch_diagk(st, op.qs, op.k, dev, ex);
+        }
+        case Q_CX:
+            return launch_cx(st, op.a, op.b);
+        default:
+            return launch_swap(st, op.a, op.b);
+    }
+}
+
+static uint64_t touch_mask(const QOp &op) {
+    if (op.kind == Q_CX || op.kind == Q_SWAP) return (1ull << op.a) | (1ull << op.b);
+    uint64_t m = 0;
+    for (uint32_t i = 0; i < op.k; i++) m |= 1ull << op.qs[i];
+    return m;
+}
+
+// Qubits that must be local for `op` to run inside a sweep.
+static uint64_t need_mask(const QOp &op) {
+    switch (op.kind) {
+        case Q_UNITARY: return 1ull << op.qs[0];
+        case Q_DIAG: return 0;
+        case Q_CX: return 1ull << op.b;
+        default: return (1ull << op.a) | (1ull << op.b);
+    }
+}
+
+static bool sweepable(const QOp &op) { return !(op.kind == Q_UNITARY && op.k > 1); }
+
+struct SweepShape {
+    uint32_t L, Hcap;
+};
+
+static SweepShape shape_for(const zc_state *st) {
+    const uint32_t L = std::min<uint32_t>(st->n, st->prec == 64 ? 5 : 6);  // 256-byte rows
+    const uint32_t Tmax = st->prec == 64 ? 12 : 13;                       // 64 KiB per tile buffer
+    uint32_t Hcap = std::min<uint32_t>(Tmax - L, st->n - L);
+    // keep at least ~2 tiles per SM so every SM streams
+    uint32_t tiles_log2 = 0;
+    while ((1u << tiles_log2) < (uint32_t)(2 * st->num_sms)) tiles_log2++;
+    if (st->n - L > tiles_log2) Hcap = std::min<uint32_t>(Hcap, st->n - L - tiles_log2);
+    else Hcap = 0;
+    return SweepShape{L, Hcap};
+}
+
+static uint32_t loc_of(uint32_t q, uint32_t L, const std::vector<uint32_t> &highs) {
+    if (q < L) return q;
+    for (size_t j = 0; j < highs.size(); j++)
+        if (highs[j] == q) return L + (uint32_t)j;
+    return kOuterFlag | q;
+}
+
+// Plan and launch one sweep starting at the queue front; erases what ran.
+static int run_one_sweep(zc_state *st) {
+    std::vector<QOp> &q = st->queue;
+    const SweepShape sh = shape_for(st);
+    const bool ex = exact(st);
+    const uint64_t low_mask = sh.L >= 64 ? ~0ull : ((1ull << sh.L) - 1);
+    uint64_t blocked = 0, highs_mask = 0;
+    uint32_t nhigh = 0;
+    bool arith_deferred = false;
+    std::vector<size_t> taken;
+    const size_t window = std::min(q.size(), kQueueWindow);
+    for (size_t i = 0; i < window && taken.size() < (size_t)kMaxMicroOps; i++) {
+        const QOp &op = q[i];
+        const uint64_t touch = touch_mask(op);
+        const bool arith = op.kind == Q_UNITARY || op.kind == Q_DIAG;
+        bool defer = (touch & blocked) != 0 || (ex && arith && arith_deferred) || !sweepable(op);
+        uint64_t need = 0;
+        if (!defer) {
+            need = need_mask(op) & ~low_mask & ~highs_mask;
+            if (nhigh + (uint32_t)__builtin_popcountll(need) > sh.Hcap) defer = true;
+        }
+        if (defer) {
+            blocked |= touch;
+            arith_deferred |= arith;
+            continue;
+        }
+        highs_mask |= need;
+        nhigh += (uint32_t)__builtin_popcountll(need);
+        taken.push_back(i);
+    }
+    if (taken.size() <= 1) {
+        // nothing to batch: the per-op kernel is the same work
+        int rc = launch_single(st, q.front());
+        q.erase(q.begin());
+        return rc;
+    }
+    // pad the tile with further high qubits up to the cap (no effect on results)
+    for (uint32_t b = sh.L; b < st->n && nhigh < sh.Hcap; b++)
+        if (!((highs_mask >> b) & 1)) {
+            highs_mask |= 1ull << b;
+            nhigh++;
+        }
+    std::vector<uint32_t> highs;
+    for (uint32_t b = 0; b < st->n; b++)
+        if ((highs_mask >> b) & 1) highs.push_back(b);
+    SweepGeom g{};
+    g.n = st->n;
+    g.L = sh.L;
+    g.H = (uint32_t)highs.size();
+    for (size_t j = 0; j < highs.size(); j++) g.hpos[j] = highs[j];
+    g.ntiles = 1ull << (st->n - g.L - g.H);
+    // encode: [MicroOp x nops][tables...]
+    std::vector<MicroOp> mops(taken.size());
+    std::vector<char> tables;
+    const size_t es = st->prec / 8;
+    for (size_t t = 0; t < taken.size(); t++) {
+        const QOp &op = q[taken[t]];
+        MicroOp &m = mops[t];
+        memset(&m, 0, sizeof m);
+        if (op.kind == Q_UNITARY) {
+            m.kind = MOP_U1;
+            m.a = loc_of(op.qs[0], g.L, highs);
+            for (int i = 0; i < 8; i++) m.m[i] = op.data[i];
+        } else if (op.kind == Q_DIAG && op.k == 1) {
+            m.kind = MOP_D1;
+            m.a = loc_of(op.qs[0], g.L, highs);
+            for (int i = 0; i < 4; i++) m.m[i] = op.data[i];
+        } else if (op.kind == Q_DIAG) {
+            m.kind = MOP_DK;
+            m.k = op.k;
+            for (uint32_t b = 0; b < op.k; b++) m.loc[b] = loc_of(op.qs[b], g.L, highs);
+            const size_t dim = (size_t)1 << op.k;
+            size_t off = (tables.size() + 15) & ~(size_t)15;
+            tables.resize(off + 2 * dim * es);
+            for (size_t j = 0; j < dim; j++) {
+                if (es == 8) {
+                    ((double *)(tables.data() + off))[j] = op.data[2 * j];
+                    ((double *)(tables.data() + off))[dim + j] = op.data[2 * j + 1];
+                } else {
+                    ((float *)(tables.data() + off))[j] = (float)op.data[2 * j];
+                    ((float *)(tables.data() + off))[dim + j] = (float)op.data[2 * j + 1];
+                }
+            }
+            m.table = off;
+        } else if (op.kind == Q_CX) {
+            m.kind = MOP_CX;
+            m.a = loc_of(op.a, g.L, highs);
+            m.b = loc_of(op.b, g.L, highs);
+        } else {
+            m.kind = MOP_SWAP;
+            m.a = loc_of(op.a, g.L, highs);
+            m.b = loc_of(op.b, g.L, highs);
+        }
+    }
+    const size_t ops_bytes = mops.size() * sizeof(MicroOp);
+    const size_t tab_off = (ops_bytes + 255) & ~(size_t)255;
+    std::vector<char> blob(tab_off + tables.size());
+    memcpy(blob.data(), mops.data(), ops_bytes);
+    if (!tables.empty()) memcpy(blob.data() + tab_off, tables.data(), tables.size());
+    const void *dev = nullptr;
+    int rc = arena_put(st, blob.data(), blob.size(), &dev);
+    if (rc) return rc;
+    rc = launch_sweep(st, g, (const MicroOp *)dev, (int)mops.size(), (const char *)dev + tab_off, ex);
+    // drop the ops that ran (indices ascending)
+    std::vector<QOp> rest;
+    rest.reserve(q.size() - taken.size());
+    size_t ti = 0;
+    for (size_t i = 0; i < q.size(); i++) {
+        if (ti < taken.size() && taken[ti] == i) {
+            ti++;
+            continue;
+        }
+        rest.push_back(std::move(q[i]));
+    }
+    q.swap(rest);
+    return rc;
+}
+
+static bool sweeps_enabled(const zc_state *st) {
+    if (st->flags & ZC_FLAG_NO_SWEEPS) return false;
+    if (st->flags & ZC_FLAG_FORCE_SWEEPS) return st->n >= 3;
+    return st->n >= kMinSweepQubits;
+}
+
+// Launch everything queued (program order preserved where results depend on it).
+static int flush(zc_state *st) {
+    int rc = ZC_OK;
+    while (!st->queue.empty() && rc == ZC_OK) {
+        if (!sweeps_enabled(st) || !sweepable(st->queue.front())) {
+            rc = launch_single(st, st->queue.front());
+            st->queue.erase(st->queue.begin());
+            continue;
+        }
+        rc = run_one_sweep(st);
+    }
+    st->queue.clear();
+    return rc;
+}
+
+static int enqueue(zc_state *st, QOp &&op) {
+    st->ctr.ops++;
+    if (!sweeps_enabled(st)) return launch_single(st, op);
+    st->queue.push_back(std::move(op));
+    if (st->queue.size() >= kQueueFlushAt) return flush(st);
+    return ZC_OK;
+}
+
+static int check_device_error(zc_state *st) {
+    int h = 0;
+    ZC_CUDA(cudaMemcpyAsync(&h, st->d_err, sizeof(int), cudaMemcpyDeviceToHost, st->stream));
+    ZC_CUDA(cudaStreamSynchronize(st->stream));
+    if (h) {
+        cudaMemsetAsync(st->d_err, 0, sizeof(int), st->stream);
+        return fail(ZC_ERR_CUDA, "sweep kernel gave up waiting for a bulk copy (device wait limit reached)");
+    }
+    return ZC_OK;
+}
+
 }  // namespace zc
 
 using namespace zc;
@@ -202,6 +434,8 @@ int zc_create_ex(uint32_t n, int prec, uint32_t flags, zc_state **out) {
     TRY(cudaMalloc(&st->arena.dev, kArenaBytes));
     st->arena.cap = kArenaBytes;
     TRY(cudaMalloc(&st->d_scalar, sizeof(double)));
+    TRY(cudaMalloc(&st->d_err, sizeof(int)));
+    TRY(cudaMemsetAsync(st->d_err, 0, sizeof(int), st->stream));
     TRY(cudaMallocHost(&st->h_scalar, sizeof(double)));
 #undef TRY
     rc = launch_reset(st);
@@ -224,6 +458,7 @@ void zc_destroy(zc_state *st) {
     if (st->d_scalar) cudaFree(st->d_scalar);
     if (st->h_scalar) cudaFreeHost(st->h_scalar);
     if (st->d_samp) cudaFree(st->d_samp);
+    if (st->d_err) cudaFree(st->d_err);
     if (st->stream) cudaStreamDestroy(st->stream);
     delete st;
 }
@@ -234,46 +469,39 @@ int zc_apply_unitary(zc_state *st, const uint32_t *qs, uint32_t k, const double 
     int rc = check_support(st, qs, k, kMaxUnitaryQubits, "apply_unitary");
     if (rc) return rc;
     if (!mat) return fail(ZC_ERR_INVALID, "apply_unitary: null matrix");
-    st->ctr.ops++;
-    if (k == 1) return launch_1q(st, qs[0], mat, exact(st));
-    const void *dev = nullptr;
-    rc = stage_table(st, mat, (size_t)1 << (2 * k), &dev);
-    if (rc) return rc;
-    return launch_kq(st, qs, k, dev, exact(st));
+    QOp op{Q_UNITARY, k, {}, 0, 0, std::vector<double>(mat, mat + 2 * ((size_t)1 << (2 * k)))};
+    for (uint32_t i = 0; i < k; i++) op.qs[i] = qs[i];
+    return enqueue(st, std::move(op));
 }
 
 int zc_apply_diagonal(zc_state *st, const uint32_t *qs, uint32_t k, const double *d) {
     int rc = check_support(st, qs, k, kMaxDiagQubits, "apply_diagonal");
     if (rc) return rc;
     if (!d) return fail(ZC_ERR_INVALID, "apply_diagonal: null diagonal");
-    st->ctr.ops++;
-    if (k == 1) return launch_diag1(st, qs[0], d, exact(st));
-    const void *dev = nullptr;
-    rc = stage_table(st, d, (size_t)1 << k, &dev);
-    if (rc) return rc;
-    return launch_diagk(st, qs, k, dev, exact(st));
+    QOp op{Q_DIAG, k, {}, 0, 0, std::vector<double>(d, d + 2 * ((size_t)1 << k))};
+    for (uint32_t i = 0; i < k; i++) op.qs[i] = qs[i];
+    return enqueue(st, std::move(op));
 }
 
 int zc_apply_cx(zc_state *st, uint32_t c, uint32_t t) {
     if (!st) return fail(ZC_ERR_INVALID, "null state");
     if (c >= st->n || t >= st->n || c == t) return fail(ZC_ERR_INVALID, "apply_cx: bad control/target");
-    if (st->n < 2) return fail(ZC_ERR_INVALID, "apply_cx: needs two qubits");
-    st->ctr.ops++;
-    return launch_cx(st, c, t);
+    return enqueue(st, QOp{Q_CX, 0, {}, c, t, {}});
 }
 
 int zc_apply_swap(zc_state *st, uint32_t a, uint32_t b) {
     if (!st) return fail(ZC_ERR_INVALID, "null state");
     if (a >= st->n || b >= st->n || a == b) return fail(ZC_ERR_INVALID, "apply_swap: bad qubits");
-    st->ctr.ops++;
-    return launch_swap(st, a, b);
+    return enqueue(st, QOp{Q_SWAP, 0, {}, std::min(a, b), std::max(a, b), {}});
 }
 
 int zc_prob_one(zc_state *st, uint32_t q, double *out) {
     if (!st || !out) return fail(ZC_ERR_INVALID, "null argument");
     if (q >= st->n) return fail(ZC_ERR_INVALID, "prob_one: qubit out of range");
+    int rc = flush(st);
+    if (rc) return rc;
     size_t nch = 0;
-    int rc = launch_chunk_sums(st, 1, q, &nch);
+    rc = launch_chunk_sums(st, 1, q, &nch);
     if (rc) return rc;
     rc = launch_serial_sum(st, nch);
     if (rc) return rc;
@@ -295,13 +523,16 @@ int zc_measure(zc_state *st, uint32_t q, double u, int *outcome) {
 
 int zc_reset_all(zc_state *st) {
     if (!st) return fail(ZC_ERR_INVALID, "null state");
+    st->queue.clear();  // queued ops act on a state that is being discarded
     return launch_reset(st);
 }
 
 int zc_norm_sqr(zc_state *st, double *out) {
     if (!st || !out) return fail(ZC_ERR_INVALID, "null argument");
+    int rc = flush(st);
+    if (rc) return rc;
     size_t nch = 0;
-    int rc = launch_chunk_sums(st, 0, 0, &nch);
+    rc = launch_chunk_sums(st, 0, 0, &nch);
     if (rc) return rc;
     rc = launch_serial_sum(st, nch);
     if (rc) return rc;
@@ -315,8 +546,10 @@ int zc_sample(zc_state *st, uint64_t shots, uint64_t seed, uint64_t *out) {
     if (!st) return fail(ZC_ERR_INVALID, "null state");
     if (shots == 0) return ZC_OK;
     if (!out) return fail(ZC_ERR_INVALID, "sample: null output");
+    int rc = flush(st);
+    if (rc) return rc;
     size_t nch = 0;
-    int rc = launch_chunk_sums(st, 0, 0, &nch);
+    rc = launch_chunk_sums(st, 0, 0, &nch);
     if (rc) return rc;
     std::vector<double> sums(nch);
     ZC_CUDA(cudaMemcpyAsync(sums.data(), st->d_part, nch * sizeof(double), cudaMemcpyDeviceToHost, st->stream));
@@ -358,6 +591,8 @@ int zc_sample(zc_state *st, uint64_t shots, uint64_t seed, uint64_t *out) {
 
 int zc_statevector(zc_state *st, double *out) {
     if (!st || !out) return fail(ZC_ERR_INVALID, "null argument");
+    int rc = flush(st);
+    if (rc) return rc;
     const size_t es = st->prec / 8;
     std::vector<char> re(st->len * es), im(st->len * es);
     ZC_CUDA(cudaMemcpyAsync(re.data(), st->re, st->len * es, cudaMemcpyDeviceToHost, st->stream));
@@ -377,6 +612,7 @@ int zc_statevector(zc_state *st, double *out) {
 
 int zc_load_state(zc_state *st, const double *in) {
     if (!st || !in) return fail(ZC_ERR_INVALID, "null argument");
+    st->queue.clear();
     const size_t es = st->prec / 8;
     std::vector<char> re(st->len * es), im(st->len * es);
     for (size_t i = 0; i < st->len; i++) {
@@ -396,9 +632,11 @@ int zc_load_state(zc_state *st, const double *in) {
 
 int zc_finish(zc_state *st) {
     if (!st) return fail(ZC_ERR_INVALID, "null state");
+    int rc = flush(st);
+    if (rc) return rc;
     ZC_CUDA(cudaStreamSynchronize(st->stream));
     ZC_CUDA(cudaGetLastError());
-    return ZC_OK;
+    return check_device_error(st);
 }
 
 int zc_get_stream(zc_state *st, void **stream) {

@@ -93,6 +93,172 @@ __device__ __forceinline__ void cmac(T wr, T wi, T xr, T xi, T &ar, T &ai) {
     }
 }
 
+// ------------------------------------------------------------------
+// Double-float arithmetic for f64 states (fast mode).
+//
+// GB300 issues FP64 at 1/64 of the FP32 rate, so the f64 kernels' fast
+// mode keeps the state in f64 in HBM but does the gate arithmetic on the
+// FP32 pipe with unevaluated (hi, lo) float pairs (Dekker 1971; error-free
+// TwoSum of Knuth, two-product via FMA). Conversions between f64 and the
+// pair use integer bit operations only, never the FP64 pipe. A gate costs
+// about 43 FP32 operations per output component and carries ~2^-46
+// relative error; the f64 <-> pair round trip truncates at 2^-47 and
+// 2^-52. Zero, subnormals and |x| < 2^-126 map to 0.
+
+// f64 -> (hi, lo): hi = x truncated to 24 bits, lo = the next 23 bits.
+__device__ __forceinline__ float2 df_from_f64(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned hw = (unsigned)(b >> 32), lw = (unsigned)b;
+    const int e = (int)((hw >> 20) & 0x7ff);
+    const unsigned sign = hw & 0x80000000u;
+    const int ef = e - 896;   // f32 exponent field of hi
+    const int efl = e - 919;  // exponent placing the low bits below hi
+    const unsigned mant23 = ((hw & 0xfffffu) << 3) | (lw >> 29);
+    float hi = 0.0f, lo = 0.0f;
+    if (ef >= 1 && ef <= 254) hi = __uint_as_float(sign | ((unsigned)ef << 23) | mant23);
+    if (efl >= 1 && ef <= 254) {
+        const unsigned top = sign | ((unsigned)efl << 23);
+        lo = __fsub_rn(__uint_as_float(top | ((lw >> 6) & 0x7fffffu)), __uint_as_float(top));
+    }
+    return make_float2(hi, lo);
+}
+
+// (hi, lo) -> f64 with |lo| <= ulp(hi): 53-bit integer sum, truncated.
+__device__ __forceinline__ double df_to_f64(float2 v) {
+    const unsigned hb = __float_as_uint(v.x);
+    const int eh = (int)((hb >> 23) & 0xff);
+    if (eh == 0) return 0.0;
+    const unsigned long long sh = hb & 0x80000000u;
+    unsigned long long M = (unsigned long long)((hb & 0x7fffffu) | 0x800000u) << 29;
+    const unsigned lb = __float_as_uint(v.y);
+    const int el = (int)((lb >> 23) & 0xff);
+    if (el != 0) {
+        const unsigned long long ml = (lb & 0x7fffffu) | 0x800000u;
+        const int d = el - eh + 29;
+        const unsigned long long L = d >= 0 ? (ml << (d > 10 ? 10 : d)) : (d > -40 ? (ml >> -d) : 0ull);
+        if ((lb & 0x80000000u) == (unsigned)sh) M += L;
+        else M -= L;
+    }
+    int E = eh + 896;
+    if (M >> 53) {
+        M >>= 1;
+        E += 1;
+    } else if (!(M >> 52)) {
+        M <<= 1;
+        E -= 1;
+    }
+    return __longlong_as_double((long long)((sh << 32) | ((unsigned long long)E << 52) | (M & 0xfffffffffffffull)));
+}
+
+// Exact product split: a*b = p + e with e from one FMA, plus cross terms.
+__device__ __forceinline__ void df_prod(float2 a, float2 b, float &p, float &e) {
+    p = __fmul_rn(a.x, b.x);
+    e = __fmaf_rn(a.x, b.x, -p);
+    e = __fmaf_rn(a.x, b.y, e);
+    e = __fmaf_rn(a.y, b.x, e);
+}
+
+// s + err = a + b exactly (TwoSum).
+__device__ __forceinline__ float two_sum(float a, float b, float &err) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    err = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return s;
+}
+
+__device__ __forceinline__ float2 df_norm(float s, float lo) {
+    const float h = __fadd_rn(s, lo);
+    return make_float2(h, __fsub_rn(lo, __fsub_rn(h, s)));
+}
+
+__device__ __forceinline__ float2 df_neg(float2 a) { return make_float2(-a.x, -a.y); }
+
+// x0*y0 + x1*y1 + x2*y2 + x3*y3 in double-float.
+__device__ __forceinline__ float2 df_dot4(float2 x0, float2 y0, float2 x1, float2 y1, float2 x2, float2 y2, float2 x3,
+                                          float2 y3) {
+    float p0, e0, p1, e1, p2, e2, p3, e3, r1, r2, r3;
+    df_prod(x0, y0, p0, e0);
+    df_prod(x1, y1, p1, e1);
+    df_prod(x2, y2, p2, e2);
+    df_prod(x3, y3, p3, e3);
+    float s = two_sum(p0, p1, r1);
+    s = two_sum(s, p2, r2);
+    s = two_sum(s, p3, r3);
+    const float lo = __fadd_rn(__fadd_rn(__fadd_rn(r1, r2), r3), __fadd_rn(__fadd_rn(e0, e1), __fadd_rn(e2, e3)));
+    return df_norm(s, lo);
+}
+
+__device__ __forceinline__ float2 df_dot2(float2 x0, float2 y0, float2 x1, float2 y1) {
+    float p0, e0, p1, e1, r1;
+    df_prod(x0, y0, p0, e0);
+    df_prod(x1, y1, p1, e1);
+    const float s = two_sum(p0, p1, r1);
+    return df_norm(s, __fadd_rn(r1, __fadd_rn(e0, e1)));
+}
+
+// Gate matrix in double-float: m00r m00i m01r m01i m10r m10i m11r m11i.
+struct MatDF {
+    float2 v[8];
+};
+
+// Host-exact split of the f64 entries happens on the device once per op.
+__device__ __forceinline__ MatDF df_matrix(const double *m) {
+    MatDF r;
+#pragma unroll
+    for (int i = 0; i < 8; i++) r.v[i] = df_from_f64(m[i]);
+    return r;
+}
+
+// 2x2 complex update of (a, b) in double-float (same formula as pair_update).
+__device__ __forceinline__ void pair_update_df(const MatDF &m, float2 &ar, float2 &ai, float2 &br, float2 &bi) {
+    const float2 nar = df_dot4(m.v[0], ar, df_neg(m.v[1]), ai, m.v[2], br, df_neg(m.v[3]), bi);
+    const float2 nai = df_dot4(m.v[0], ai, m.v[1], ar, m.v[2], bi, m.v[3], br);
+    const float2 nbr = df_dot4(m.v[4], ar, df_neg(m.v[5]), ai, m.v[6], br, df_neg(m.v[7]), bi);
+    const float2 nbi = df_dot4(m.v[4], ai, m.v[5], ar, m.v[6], bi, m.v[7], br);
+    ar = nar;
+    ai = nai;
+    br = nbr;
+    bi = nbi;
+}
+
+__device__ __forceinline__ void cscale_df(float2 wr, float2 wi, float2 &ar, float2 &ai) {
+    const float2 nr = df_dot2(wr, ar, df_neg(wi), ai);
+    const float2 ni = df_dot2(wr, ai, wi, ar);
+    ar = nr;
+    ai = ni;
+}
+
+// Arithmetic policies: 0 = exact reference trees, 1 = FMA-contracted,
+// 2 = double-float on the FP32 pipe (f64 states only).
+enum : int { AR_EXACT = 0, AR_FMA = 1, AR_DF = 2 };
+
+// pair_update under policy A on values stored as T.
+template <typename T, int A>
+__device__ __forceinline__ void upd2(const Mat2<T> &m, const MatDF &md, T &ar, T &ai, T &br, T &bi) {
+    if constexpr (A == AR_DF) {
+        float2 xr = df_from_f64(ar), xi = df_from_f64(ai), yr = df_from_f64(br), yi = df_from_f64(bi);
+        pair_update_df(md, xr, xi, yr, yi);
+        ar = df_to_f64(xr);
+        ai = df_to_f64(xi);
+        br = df_to_f64(yr);
+        bi = df_to_f64(yi);
+    } else {
+        pair_update<T, A == AR_EXACT>(m, ar, ai, br, bi);
+    }
+}
+
+template <typename T, int A>
+__device__ __forceinline__ void scale2(T wr, T wi, float2 wrd, float2 wid, T &ar, T &ai) {
+    if constexpr (A == AR_DF) {
+        float2 xr = df_from_f64(ar), xi = df_from_f64(ai);
+        cscale_df(wrd, wid, xr, xi);
+        ar = df_to_f64(xr);
+        ai = df_to_f64(xi);
+    } else {
+        cscale<T, A == AR_EXACT>(wr, wi, ar, ai);
+    }
+}
+
 // insert_zeros (src/state.rs:162-169): spread g around zero bits at the
 // ascending positions qs[0..k).
 __device__ __forceinline__ uint64_t insert_zeros(uint64_t g, const uint32_t *qs, int k) {

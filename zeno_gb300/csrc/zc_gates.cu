@@ -25,10 +25,12 @@ Launch grid_for(const zc_state *st, uint64_t units) {
 // q such that 2^q >= V: every thread owns V consecutive half indices, so
 // the a-row and b-row loads are 16-byte vectors and a warp reads two
 // contiguous 512-byte spans (kern_1q_scalar, src/state.rs:232-260).
-template <typename T, bool EXACT>
+template <typename T, int A>
 __global__ void __launch_bounds__(kThreads) k_1q_rows(T *__restrict__ re, T *__restrict__ im, uint32_t q,
                                                       uint64_t nunits, Mat2<T> m) {
     constexpr int V = Vec<T>::N;
+    MatDF md;
+    if constexpr (A == AR_DF) md = df_matrix(reinterpret_cast<const double *>(m.v));
     using VT = typename Vec<T>::type;
     const uint64_t s = 1ull << q;
     for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < nunits;
@@ -41,7 +43,7 @@ __global__ void __launch_bounds__(kThreads) k_1q_rows(T *__restrict__ re, T *__r
         T *ar = reinterpret_cast<T *>(&var), *ai = reinterpret_cast<T *>(&vai);
         T *br = reinterpret_cast<T *>(&vbr), *bi = reinterpret_cast<T *>(&vbi);
 #pragma unroll
-        for (int e = 0; e < V; e++) pair_update<T, EXACT>(m, ar[e], ai[e], br[e], bi[e]);
+        for (int e = 0; e < V; e++) upd2<T, A>(m, md, ar[e], ai[e], br[e], bi[e]);
         *reinterpret_cast<VT *>(re + a) = var;
         *reinterpret_cast<VT *>(im + a) = vai;
         *reinterpret_cast<VT *>(re + a + s) = vbr;
@@ -50,10 +52,12 @@ __global__ void __launch_bounds__(kThreads) k_1q_rows(T *__restrict__ re, T *__r
 }
 
 // 2^q < V: both members of every pair sit inside one 16-byte vector.
-template <typename T, bool EXACT>
+template <typename T, int A>
 __global__ void __launch_bounds__(kThreads) k_1q_inreg(T *__restrict__ re, T *__restrict__ im, uint32_t q,
                                                        uint64_t nunits, Mat2<T> m) {
     constexpr int V = Vec<T>::N;
+    MatDF md;
+    if constexpr (A == AR_DF) md = df_matrix(reinterpret_cast<const double *>(m.v));
     using VT = typename Vec<T>::type;
     const int s = 1 << q;
     for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < nunits;
@@ -64,7 +68,7 @@ __global__ void __launch_bounds__(kThreads) k_1q_inreg(T *__restrict__ re, T *__
 #pragma unroll
         for (int p = 0; p < V; p++) {
             if (p & s) continue;
-            pair_update<T, EXACT>(m, r[p], i[p], r[p | s], i[p | s]);
+            upd2<T, A>(m, md, r[p], i[p], r[p | s], i[p | s]);
         }
         *reinterpret_cast<VT *>(re + u * V) = vr;
         *reinterpret_cast<VT *>(im + u * V) = vi;
@@ -72,16 +76,18 @@ __global__ void __launch_bounds__(kThreads) k_1q_inreg(T *__restrict__ re, T *__
 }
 
 // Scalar fallback for states shorter than two vectors.
-template <typename T, bool EXACT>
+template <typename T, int A>
 __global__ void k_1q_scalar(T *re, T *im, uint32_t q, uint64_t half, Mat2<T> m) {
+    MatDF md;
+    if constexpr (A == AR_DF) md = df_matrix(reinterpret_cast<const double *>(m.v));
     for (uint64_t h = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; h < half;
          h += (uint64_t)gridDim.x * blockDim.x) {
         const uint64_t a = insert_zero(h, q), b = a + (1ull << q);
-        pair_update<T, EXACT>(m, re[a], im[a], re[b], im[b]);
+        upd2<T, A>(m, md, re[a], im[a], re[b], im[b]);
     }
 }
 
-template <typename T, bool EXACT>
+template <typename T, int A>
 int run_1q(zc_state *st, uint32_t q, const double *m8) {
     constexpr int V = Vec<T>::N;
     Mat2<T> m;
@@ -89,15 +95,15 @@ int run_1q(zc_state *st, uint32_t q, const double *m8) {
     T *re = (T *)st->re, *im = (T *)st->im;
     const uint64_t len = st->len;
     if (len < 2 * (uint64_t)V) {
-        k_1q_scalar<T, EXACT><<<1, 64, 0, st->stream>>>(re, im, q, len / 2, m);
+        k_1q_scalar<T, A><<<1, 64, 0, st->stream>>>(re, im, q, len / 2, m);
     } else if ((1ull << q) >= (uint64_t)V) {
         const uint64_t nunits = len / 2 / V;
         Launch L = grid_for(st, nunits);
-        k_1q_rows<T, EXACT><<<L.blocks, L.threads, 0, st->stream>>>(re, im, q, nunits, m);
+        k_1q_rows<T, A><<<L.blocks, L.threads, 0, st->stream>>>(re, im, q, nunits, m);
     } else {
         const uint64_t nunits = len / V;
         Launch L = grid_for(st, nunits);
-        k_1q_inreg<T, EXACT><<<L.blocks, L.threads, 0, st->stream>>>(re, im, q, nunits, m);
+        k_1q_inreg<T, A><<<L.blocks, L.threads, 0, st->stream>>>(re, im, q, nunits, m);
     }
     ZC_CUDA(cudaGetLastError());
     return ZC_OK;
@@ -200,11 +206,15 @@ int run_kq(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat) {
 // ---------------------------------------------------------------- diagonals
 
 // 1-qubit diagonal (kern_diag1_scalar, src/state.rs:498-527).
-template <typename T, bool EXACT>
+template <typename T, int A>
 __global__ void __launch_bounds__(kThreads) k_diag1(T *__restrict__ re, T *__restrict__ im, uint32_t q,
                                                     uint64_t nunits, T d0r, T d0i, T d1r, T d1i) {
     constexpr int V = Vec<T>::N;
     using VT = typename Vec<T>::type;
+    float2 e0r{}, e0i{}, e1r{}, e1i{};
+    if constexpr (A == AR_DF) {
+        e0r = df_from_f64(d0r), e0i = df_from_f64(d0i), e1r = df_from_f64(d1r), e1i = df_from_f64(d1i);
+    }
     for (uint64_t u = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; u < nunits;
          u += (uint64_t)gridDim.x * blockDim.x) {
         VT vr = *reinterpret_cast<const VT *>(re + u * V);
@@ -213,18 +223,18 @@ __global__ void __launch_bounds__(kThreads) k_diag1(T *__restrict__ re, T *__res
 #pragma unroll
         for (int e = 0; e < V; e++) {
             const bool one = ((u * V + e) >> q) & 1;
-            cscale<T, EXACT>(one ? d1r : d0r, one ? d1i : d0i, r[e], i[e]);
+            scale2<T, A>(one ? d1r : d0r, one ? d1i : d0i, one ? e1r : e0r, one ? e1i : e0i, r[e], i[e]);
         }
         *reinterpret_cast<VT *>(re + u * V) = vr;
         *reinterpret_cast<VT *>(im + u * V) = vi;
     }
 }
 
-template <typename T, bool EXACT>
+template <typename T, int A>
 __global__ void k_diag1_scalar(T *re, T *im, uint32_t q, uint64_t len, T d0r, T d0i, T d1r, T d1i) {
     for (uint64_t i = threadIdx.x; i < len; i += blockDim.x) {
         const bool one = (i >> q) & 1;
-        cscale<T, EXACT>(one ? d1r : d0r, one ? d1i : d0i, re[i], im[i]);
+        cscale<T, A == AR_EXACT>(one ? d1r : d0r, one ? d1i : d0i, re[i], im[i]);
     }
 }
 
@@ -235,7 +245,7 @@ struct DiagParams {
 
 // k-qubit diagonal (kern_diagk_scalar, src/state.rs:577-596): table in
 // shared memory, j gathered from the index bits at qs.
-template <typename T, bool EXACT>
+template <typename T, int A>
 __global__ void __launch_bounds__(kThreads) k_diagk(T *__restrict__ re, T *__restrict__ im, uint64_t nunits,
                                                     DiagParams p, const T *__restrict__ dre,
                                                     const T *__restrict__ dim_) {
@@ -260,42 +270,45 @@ __global__ void __launch_bounds__(kThreads) k_diagk(T *__restrict__ re, T *__res
             const uint64_t idx = u * V + e;
             uint32_t j = 0;
             for (uint32_t b = 0; b < p.k; b++) j |= (uint32_t)((idx >> p.qs[b]) & 1) << b;
-            cscale<T, EXACT>(tr[j], ti[j], r[e], i[e]);
+            if constexpr (A == AR_DF)
+                scale2<T, A>(tr[j], ti[j], df_from_f64(tr[j]), df_from_f64(ti[j]), r[e], i[e]);
+            else
+                cscale<T, A == AR_EXACT>(tr[j], ti[j], r[e], i[e]);
         }
         *reinterpret_cast<VT *>(re + u * V) = vr;
         *reinterpret_cast<VT *>(im + u * V) = vi;
     }
 }
 
-template <typename T, bool EXACT>
+template <typename T, int A>
 __global__ void k_diag_scalar(T *re, T *im, uint64_t len, DiagParams p, const T *dre, const T *dim_) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len;
          i += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t j = 0;
         for (uint32_t b = 0; b < p.k; b++) j |= (uint32_t)((i >> p.qs[b]) & 1) << b;
-        cscale<T, EXACT>(dre[j], dim_[j], re[i], im[i]);
+        cscale<T, A == AR_EXACT>(dre[j], dim_[j], re[i], im[i]);
     }
 }
 
-template <typename T, bool EXACT>
+template <typename T, int A>
 int run_diag1(zc_state *st, uint32_t q, const double *d4) {
     constexpr int V = Vec<T>::N;
     T *re = (T *)st->re, *im = (T *)st->im;
     if (st->len < (uint64_t)V) {
-        k_diag1_scalar<T, EXACT><<<1, 32, 0, st->stream>>>(re, im, q, st->len, (T)d4[0], (T)d4[1], (T)d4[2],
+        k_diag1_scalar<T, A><<<1, 32, 0, st->stream>>>(re, im, q, st->len, (T)d4[0], (T)d4[1], (T)d4[2],
                                                            (T)d4[3]);
         ZC_CUDA(cudaGetLastError());
         return ZC_OK;
     }
     const uint64_t nunits = st->len / V;
     Launch L = grid_for(st, nunits);
-    k_diag1<T, EXACT><<<L.blocks, L.threads, 0, st->stream>>>(re, im, q, nunits, (T)d4[0], (T)d4[1], (T)d4[2],
+    k_diag1<T, A><<<L.blocks, L.threads, 0, st->stream>>>(re, im, q, nunits, (T)d4[0], (T)d4[1], (T)d4[2],
                                                                (T)d4[3]);
     ZC_CUDA(cudaGetLastError());
     return ZC_OK;
 }
 
-template <typename T, bool EXACT>
+template <typename T, int A>
 int run_diagk(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_diag) {
     constexpr int V = Vec<T>::N;
     DiagParams p{};
@@ -305,16 +318,16 @@ int run_diagk(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_diag
     const T *dre = (const T *)dev_diag, *dim_ = dre + dim;
     T *re = (T *)st->re, *im = (T *)st->im;
     if (st->len < (uint64_t)V) {
-        k_diag_scalar<T, EXACT><<<1, 64, 0, st->stream>>>(re, im, st->len, p, dre, dim_);
+        k_diag_scalar<T, A><<<1, 64, 0, st->stream>>>(re, im, st->len, p, dre, dim_);
     } else {
         static bool attr_set[2] = {false, false};
         if (!attr_set[sizeof(T) == 8]) {
-            ZC_CUDA(cudaFuncSetAttribute(k_diagk<T, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
+            ZC_CUDA(cudaFuncSetAttribute(k_diagk<T, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
             attr_set[sizeof(T) == 8] = true;
         }
         const uint64_t nunits = st->len / V;
         Launch L = grid_for(st, nunits);
-        k_diagk<T, EXACT><<<L.blocks, L.threads, 2 * dim * sizeof(T), st->stream>>>(re, im, nunits, p, dre, dim_);
+        k_diagk<T, A><<<L.blocks, L.threads, 2 * dim * sizeof(T), st->stream>>>(re, im, nunits, p, dre, dim_);
     }
     ZC_CUDA(cudaGetLastError());
     return ZC_OK;
@@ -393,8 +406,8 @@ int launch_1q(zc_state *st, uint32_t q, const double *m8, bool exact) {
     st->ctr.launches++;
     st->ctr.sweeps++;
     st->ctr.bytes_moved += 2 * st->len * (st->prec / 8) * 2;
-    if (st->prec == 64) return exact ? run_1q<double, true>(st, q, m8) : run_1q<double, false>(st, q, m8);
-    return exact ? run_1q<float, true>(st, q, m8) : run_1q<float, false>(st, q, m8);
+    if (st->prec == 64) return exact ? run_1q<double, AR_EXACT>(st, q, m8) : run_1q<double, AR_DF>(st, q, m8);
+    return exact ? run_1q<float, AR_EXACT>(st, q, m8) : run_1q<float, AR_FMA>(st, q, m8);
 }
 
 int launch_kq(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat, bool exact) {
@@ -410,8 +423,8 @@ int launch_diag1(zc_state *st, uint32_t q, const double *d4, bool exact) {
     st->ctr.launches++;
     st->ctr.sweeps++;
     st->ctr.bytes_moved += 2 * st->len * (st->prec / 8) * 2;
-    if (st->prec == 64) return exact ? run_diag1<double, true>(st, q, d4) : run_diag1<double, false>(st, q, d4);
-    return exact ? run_diag1<float, true>(st, q, d4) : run_diag1<float, false>(st, q, d4);
+    if (st->prec == 64) return exact ? run_diag1<double, AR_EXACT>(st, q, d4) : run_diag1<double, AR_DF>(st, q, d4);
+    return exact ? run_diag1<float, AR_EXACT>(st, q, d4) : run_diag1<float, AR_FMA>(st, q, d4);
 }
 
 int launch_diagk(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_diag, bool exact) {
@@ -419,8 +432,8 @@ int launch_diagk(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_d
     st->ctr.sweeps++;
     st->ctr.bytes_moved += 2 * st->len * (st->prec / 8) * 2;
     if (st->prec == 64)
-        return exact ? run_diagk<double, true>(st, qs, k, dev_diag) : run_diagk<double, false>(st, qs, k, dev_diag);
-    return exact ? run_diagk<float, true>(st, qs, k, dev_diag) : run_diagk<float, false>(st, qs, k, dev_diag);
+        return exact ? run_diagk<double, AR_EXACT>(st, qs, k, dev_diag) : run_diagk<double, AR_DF>(st, qs, k, dev_diag);
+    return exact ? run_diagk<float, AR_EXACT>(st, qs, k, dev_diag) : run_diagk<float, AR_FMA>(st, qs, k, dev_diag);
 }
 
 int launch_cx(zc_state *st, uint32_t c, uint32_t t) {

@@ -40,6 +40,16 @@ struct Launch {
     int threads;
 };
 
+// An op accepted by the ABI and not yet launched.
+enum : int { Q_UNITARY = 0, Q_DIAG = 1, Q_CX = 2, Q_SWAP = 3 };
+struct QOp {
+    int kind;
+    uint32_t k;
+    uint32_t qs[12];  // sorted support (unitary / diagonal)
+    uint32_t a, b;    // CX control/target, SWAP qubits
+    std::vector<double> data;  // interleaved c64 table
+};
+
 }  // namespace zc
 
 struct zc_state {
@@ -60,6 +70,8 @@ struct zc_state {
     double *h_scalar = nullptr;  // pinned
     void *d_samp = nullptr;      // sampler work area
     size_t samp_cap = 0;
+    int *d_err = nullptr;        // device error flag (sweep wait timeouts)
+    std::vector<zc::QOp> queue;  // ops waiting to be scheduled into sweeps
     zc_counters ctr{};
     std::string name;
 };
@@ -88,6 +100,10 @@ struct SampleChunk {
     uint64_t s0, s1; // draw range
     double cum;      // cum_before[chunk]
 };
+struct SweepGeom;
+struct MicroOp;
+int launch_sweep(zc_state *st, const SweepGeom &g, const MicroOp *dev_ops, int nops, const char *dev_tables,
+                 bool exact);
 int launch_sample_scan(zc_state *st, const SampleChunk *d_chunks, size_t nchunks, const double *d_us,
                        uint64_t *d_out, uint64_t chunk_len);
 

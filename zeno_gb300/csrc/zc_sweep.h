@@ -1,0 +1,33 @@
+// Shared definitions of the multi-op sweep kernel and its host scheduler.
+#pragma once
+#include <stddef.h>
+#include <stdint.h>
+
+namespace zc {
+
+constexpr uint32_t kOuterFlag = 0x80000000u;  // operand names a non-local qubit (global position)
+constexpr int kMaxMicroOps = 48;               // ops per sweep
+constexpr size_t kSweepSmemBytes = 200 * 1024;
+
+enum : uint32_t { MOP_U1 = 1, MOP_D1 = 2, MOP_DK = 3, MOP_CX = 4, MOP_SWAP = 5 };
+
+// Tile geometry: local qubits are 0..L-1 plus hpos[0..H) (ascending).
+struct SweepGeom {
+    uint32_t n, L, H, pad;
+    uint32_t hpos[16];
+    uint64_t ntiles;
+};
+
+// One op inside a sweep, operands as local bit indices (0..L+H) or
+// kOuterFlag | global qubit. U1: a = bit, m = 2x2 row-major (re, im);
+// D1: a = bit, m[0..4) = d0, d1; DK: k, loc[], table = byte offset of
+// [re(2^k) | im(2^k)] in the sweep's table block; CX: a = control,
+// b = target (local); SWAP: a, b local.
+struct MicroOp {
+    uint32_t kind, a, b, k;
+    uint32_t loc[12];
+    uint64_t table;
+    double m[8];
+};
+
+}  // namespace zc

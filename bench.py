@@ -44,12 +44,14 @@ def parse():
     ap.add_argument("--depth", type=int, default=40)
     ap.add_argument("--precision", type=int, default=64)
     ap.add_argument("--fusion", type=int, default=1)
-    ap.add_argument("--mode", default="exact", choices=["exact", "fast"])
+    ap.add_argument("--mode", default="fast", choices=["exact", "fast"])
     ap.add_argument("--shots", type=int, default=1024)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--cpu-layers", type=int, default=1, help="layers timed for the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-check", action="store_true", help="skip the fast-vs-exact accuracy check")
+    ap.add_argument("--check-qubits", type=int, default=26)
     return ap.parse_args()
 
 
@@ -64,8 +66,25 @@ def peaks():
 
 
 def workload_name(a):
+    arith = {"exact": "exact (reference expression trees, native FP)",
+             "fast": "fast (double-float on the FP32 pipe, f64 storage)" if a.precision == 64 else "fast (FMA)"}
     return "%dq depth-%d u3+matching-CX f%d, %d shots, fusion %d, %s arithmetic" % (
-        a.qubits, a.depth, a.precision, a.shots, a.fusion, a.mode)
+        a.qubits, a.depth, a.precision, a.shots, a.fusion, arith[a.mode])
+
+
+def accuracy_check(a, zc, C):
+    """Fast mode against exact mode (bit-identical to the FP64 oracle) on the
+    same circuit family at `check_qubits`: max |d amp| and output TVD."""
+    import numpy as np
+
+    p = C.matching_circuit(a.check_qubits, a.depth, a.seed).to_program()
+    ex = zc.run(p, shots=0, precision=a.precision, statevector=True, flags=zc.FLAG_EXACT).statevector
+    fa = zc.run(p, shots=0, precision=a.precision, statevector=True, flags=zc.FLAG_FAST).statevector
+    d = float(np.abs(ex - fa).max())
+    tvd = float(0.5 * np.abs(np.abs(ex) ** 2 - np.abs(fa) ** 2).sum())
+    return {"qubits": a.check_qubits, "depth": a.depth, "max_abs_damp": d, "tvd": tvd,
+            "reference": "exact mode (bit-identical to the FP64 oracle in the parity tests)",
+            "tolerance": {"max_abs_damp": 1e-12 if a.precision == 64 else 1e-5, "tvd": 1e-6}}
 
 
 class Clocks:
@@ -332,6 +351,8 @@ def main():
         line["e2e"] = {"value": 1.0 / statistics.median(ts), "unit": "circuits/s", "h2d_bytes_per_step": h2d,
                        "d2h_bytes_per_step": d2h, "sim_seconds": r.sim_time,
                        "path": "zc_run: allocate state, per-op host->device tables, kernels, sample, read indices"}
+    if rank == 0 and a.mode == "fast" and not a.no_check:
+        line["accuracy"] = accuracy_check(a, zc, C)
     if rank == 0 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(a)
     if rank == 0:

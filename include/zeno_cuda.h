@@ -3,7 +3,7 @@
  *
  * The plain entry points mirror zeno's `exec::Backend` trait
  * (src/exec.rs:134-162) one to one, so a Rust `CudaBackend` can implement
- * the trait with a thin `extern "C"` shim (see INTEGRATION.md). Borrowed
+ * the trait with a thin `extern "C"` shim. Borrowed
  * slices (`qs`, `mat`, `d`) are copied before a call returns. Complex
  * numbers cross as interleaved (re, im) doubles, the layout of
  * `num_complex::Complex<f64>`. Every call returns ZC_OK or an error code;

@@ -22,7 +22,8 @@
 namespace zc {
 namespace {
 
-constexpr int kSweepThreads = 512;
+constexpr int kSweepThreads = 256;
+constexpr int kSweepCtasPerSm = 3;
 constexpr unsigned kSpinLimit = 1u << 26;  // bounded mbarrier waits
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
@@ -76,44 +77,8 @@ __device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.a
 
 // Global index of the first element of tile t: the tile number fills the
 // non-local positions above the L low bits.
-__device__ __forceinline__ uint64_t tile_base(uint64_t t, const SweepGeom &g) {
-    return insert_zeros(t << g.L, g.hpos, (int)g.H);
-}
-
-__device__ __forceinline__ uint64_t row_offset(uint32_t r, const SweepGeom &g) {
-    uint64_t o = 0;
-    for (uint32_t j = 0; j < g.H; j++) o |= (uint64_t)((r >> j) & 1) << g.hpos[j];
-    return o;
-}
-
-// Issue the bulk loads of one tile (called by all lanes of warp 0).
-template <typename T>
-__device__ void issue_tile_load(const T *re, const T *im, T *sre, T *sim, uint64_t base, const SweepGeom &g,
-                                uint64_t *bar, int lane) {
-    const uint32_t rows = 1u << g.H;
-    const uint32_t row_elems = 1u << g.L;
-    const uint32_t row_bytes = row_elems * sizeof(T);
-    if (lane == 0) mbar_expect_tx(bar, 2u * rows * row_bytes);
-    __syncwarp();
-    for (uint32_t r = lane; r < rows; r += 32) {
-        const uint64_t gi = base | row_offset(r, g);
-        bulk_load(sre + (size_t)r * row_elems, re + gi, row_bytes, bar);
-        bulk_load(sim + (size_t)r * row_elems, im + gi, row_bytes, bar);
-    }
-}
-
-template <typename T>
-__device__ void issue_tile_store(T *re, T *im, const T *sre, const T *sim, uint64_t base, const SweepGeom &g,
-                                 int lane) {
-    const uint32_t rows = 1u << g.H;
-    const uint32_t row_elems = 1u << g.L;
-    const uint32_t row_bytes = row_elems * sizeof(T);
-    for (uint32_t r = lane; r < rows; r += 32) {
-        const uint64_t gi = base | row_offset(r, g);
-        bulk_store(re + gi, sre + (size_t)r * row_elems, row_bytes);
-        bulk_store(im + gi, sim + (size_t)r * row_elems, row_bytes);
-    }
-    bulk_commit();
+__device__ __forceinline__ uint64_t tile_base(uint64_t t, uint32_t L, const uint32_t *hpos, uint32_t H) {
+    return insert_zeros(t << L, hpos, (int)H);
 }
 
 // Swap the slots v0 <-> v1 of both arrays (values of any representation).
@@ -159,43 +124,76 @@ __device__ void apply_perm(T *sr, T *si, const MicroOp &op, uint64_t base, uint3
     }
 }
 
-// Double-float micro-ops on a tile whose f64 slots hold (hi, lo) pairs.
-__device__ void apply_ops_df(float2 *sr, float2 *si, const MicroOp *ops, int nops, uint64_t base,
-                             const SweepGeom &g, const char *tables) {
-    const uint32_t size = 1u << (g.L + g.H);
+// Per-op coefficients converted once per CTA into the compute representation.
+// U1: the 2x2 matrix; D1: entries 0..3 = d0r d0i d1r d1i. Double-float
+// pairs for A == AR_DF, else values of T.
+template <typename T, int A>
+struct OpCoef {
+    typename std::conditional<A == AR_DF, float2, T>::type v[8];
+};
+
+template <typename R>
+__device__ __forceinline__ uint32_t jgather(const MicroOp &op, uint32_t jo, uint32_t v) {
+    uint32_t j = jo;
+    for (uint32_t b = 0; b < op.k; b++)
+        if (!(op.loc[b] & kOuterFlag)) j |= ((v >> op.loc[b]) & 1) << b;
+    return j;
+}
+
+__device__ __forceinline__ uint32_t jouter(const MicroOp &op, uint64_t base) {
+    uint32_t jo = 0;
+    for (uint32_t b = 0; b < op.k; b++)
+        if (op.loc[b] & kOuterFlag) jo |= (uint32_t)((base >> (op.loc[b] & ~kOuterFlag)) & 1) << b;
+    return jo;
+}
+
+// Apply the sweep's micro-ops to one tile. For A == AR_DF the tile's f64
+// slots hold (hi, lo) float pairs (R = float2); otherwise R = T.
+template <typename T, int A, typename R>
+__device__ void apply_ops(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *coef, int nops, uint64_t base,
+                          uint32_t size, const char *tables) {
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int o = 0; o < nops; o++) {
         const MicroOp &op = ops[o];
         if (op.kind == MOP_U1) {
-            const MatDF m = df_matrix(op.m);
             const uint32_t b = op.a;
-            for (uint32_t p = tid; p < size / 2; p += nt) {
-                const uint32_t v0 = ((p >> b) << (b + 1)) | (p & ((1u << b) - 1)), v1 = v0 | (1u << b);
-                pair_update_df(m, sr[v0], si[v0], sr[v1], si[v1]);
-            }
-        } else if (op.kind == MOP_D1) {
-            const float2 d0r = df_from_f64(op.m[0]), d0i = df_from_f64(op.m[1]);
-            const float2 d1r = df_from_f64(op.m[2]), d1i = df_from_f64(op.m[3]);
-            if (op.a & kOuterFlag) {
-                const bool one = (base >> (op.a & ~kOuterFlag)) & 1;
-                for (uint32_t v = tid; v < size; v += nt) cscale_df(one ? d1r : d0r, one ? d1i : d0i, sr[v], si[v]);
+            if constexpr (A == AR_DF) {
+                MatDF m;
+#pragma unroll
+                for (int i = 0; i < 8; i++) m.v[i] = coef[o].v[i];
+                for (uint32_t p = tid; p < size / 2; p += nt) {
+                    const uint32_t v0 = ((p >> b) << (b + 1)) | (p & ((1u << b) - 1)), v1 = v0 | (1u << b);
+                    pair_update_df(m, sr[v0], si[v0], sr[v1], si[v1]);
+                }
             } else {
-                for (uint32_t v = tid; v < size; v += nt) {
-                    const bool one = (v >> op.a) & 1;
-                    cscale_df(one ? d1r : d0r, one ? d1i : d0i, sr[v], si[v]);
+                Mat2<T> m;
+#pragma unroll
+                for (int i = 0; i < 8; i++) m.v[i] = coef[o].v[i];
+                for (uint32_t p = tid; p < size / 2; p += nt) {
+                    const uint32_t v0 = ((p >> b) << (b + 1)) | (p & ((1u << b) - 1)), v1 = v0 | (1u << b);
+                    pair_update<T, A == AR_EXACT>(m, sr[v0], si[v0], sr[v1], si[v1]);
                 }
             }
-        } else if (op.kind == MOP_DK) {
-            const double *dre = reinterpret_cast<const double *>(tables + op.table);
-            const double *dim_ = dre + (1u << op.k);
-            uint32_t jo = 0;
-            for (uint32_t b = 0; b < op.k; b++)
-                if (op.loc[b] & kOuterFlag) jo |= (uint32_t)((base >> (op.loc[b] & ~kOuterFlag)) & 1) << b;
+        } else if (op.kind == MOP_D1) {
+            const bool outer = op.a & kOuterFlag;
+            const bool tile_one = outer && ((base >> (op.a & ~kOuterFlag)) & 1);
             for (uint32_t v = tid; v < size; v += nt) {
-                uint32_t j = jo;
-                for (uint32_t b = 0; b < op.k; b++)
-                    if (!(op.loc[b] & kOuterFlag)) j |= ((v >> op.loc[b]) & 1) << b;
-                cscale_df(df_from_f64(__ldg(dre + j)), df_from_f64(__ldg(dim_ + j)), sr[v], si[v]);
+                const bool one = outer ? tile_one : ((v >> op.a) & 1);
+                if constexpr (A == AR_DF)
+                    cscale_df(coef[o].v[one ? 2 : 0], coef[o].v[one ? 3 : 1], sr[v], si[v]);
+                else
+                    cscale<T, A == AR_EXACT>(coef[o].v[one ? 2 : 0], coef[o].v[one ? 3 : 1], sr[v], si[v]);
+            }
+        } else if (op.kind == MOP_DK) {
+            const uint32_t jo = jouter(op, base);
+            const T *dre = reinterpret_cast<const T *>(tables + op.table);
+            const T *dim_ = dre + (1u << op.k);
+            for (uint32_t v = tid; v < size; v += nt) {
+                const uint32_t j = jgather<R>(op, jo, v);
+                if constexpr (A == AR_DF)
+                    cscale_df(df_from_f64(__ldg(dre + j)), df_from_f64(__ldg(dim_ + j)), sr[v], si[v]);
+                else
+                    cscale<T, A == AR_EXACT>(__ldg(dre + j), __ldg(dim_ + j), sr[v], si[v]);
             }
         } else {
             apply_perm(sr, si, op, base, size);
@@ -204,116 +202,73 @@ __device__ void apply_ops_df(float2 *sr, float2 *si, const MicroOp *ops, int nop
     }
 }
 
-// Apply the sweep's micro-ops to one tile held in shared memory.
+// One CTA streams tiles through a single shared-memory buffer; three CTAs
+// per SM overlap one tile's TMA traffic with the others' arithmetic.
 template <typename T, int A>
-__device__ void apply_ops(T *sr, T *si, const MicroOp *ops, int nops, uint64_t base, const SweepGeom &g,
-                          const char *tables) {
-    constexpr bool EXACT = A == AR_EXACT;
-    const uint32_t Tb = g.L + g.H;
-    const uint32_t size = 1u << Tb;
-    const int tid = threadIdx.x, nt = blockDim.x;
-    for (int o = 0; o < nops; o++) {
-        const MicroOp &op = ops[o];
-        switch (op.kind) {
-            case MOP_U1: {
-                Mat2<T> m;
-#pragma unroll
-                for (int i = 0; i < 8; i++) m.v[i] = (T)op.m[i];
-                const uint32_t b = op.a;
-                for (uint32_t p = tid; p < size / 2; p += nt) {
-                    const uint32_t v0 = ((p >> b) << (b + 1)) | (p & ((1u << b) - 1)), v1 = v0 | (1u << b);
-                    pair_update<T, EXACT>(m, sr[v0], si[v0], sr[v1], si[v1]);
-                }
-                break;
-            }
-            case MOP_D1: {
-                const T d0r = (T)op.m[0], d0i = (T)op.m[1], d1r = (T)op.m[2], d1i = (T)op.m[3];
-                if (op.a & kOuterFlag) {
-                    const bool one = (base >> (op.a & ~kOuterFlag)) & 1;
-                    const T wr = one ? d1r : d0r, wi = one ? d1i : d0i;
-                    for (uint32_t v = tid; v < size; v += nt) cscale<T, EXACT>(wr, wi, sr[v], si[v]);
-                } else {
-                    for (uint32_t v = tid; v < size; v += nt) {
-                        const bool one = (v >> op.a) & 1;
-                        cscale<T, EXACT>(one ? d1r : d0r, one ? d1i : d0i, sr[v], si[v]);
-                    }
-                }
-                break;
-            }
-            case MOP_DK: {
-                const T *dre = reinterpret_cast<const T *>(tables + op.table);
-                const T *dim_ = dre + (1u << op.k);
-                uint32_t jo = 0;
-                for (uint32_t b = 0; b < op.k; b++)
-                    if (op.loc[b] & kOuterFlag) jo |= (uint32_t)((base >> (op.loc[b] & ~kOuterFlag)) & 1) << b;
-                for (uint32_t v = tid; v < size; v += nt) {
-                    uint32_t j = jo;
-                    for (uint32_t b = 0; b < op.k; b++)
-                        if (!(op.loc[b] & kOuterFlag)) j |= ((v >> op.loc[b]) & 1) << b;
-                    cscale<T, EXACT>(__ldg(dre + j), __ldg(dim_ + j), sr[v], si[v]);
-                }
-                break;
-            }
-            case MOP_CX:
-            case MOP_SWAP:
-                apply_perm(sr, si, op, base, size);
-                break;
-            default:
-                break;
-        }
-        __syncthreads();
-    }
-}
-
-template <typename T, int A>
-__global__ void __launch_bounds__(kSweepThreads, 1)
+__global__ void __launch_bounds__(kSweepThreads, kSweepCtasPerSm)
     k_sweep(T *__restrict__ re, T *__restrict__ im, const SweepGeom g, const MicroOp *__restrict__ gops, int nops,
             const char *__restrict__ tables, int *__restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bars[2];
+    __shared__ __align__(8) uint64_t bar;
     __shared__ MicroOp ops[kMaxMicroOps];
+    __shared__ OpCoef<T, A> coef[kMaxMicroOps];
+    __shared__ uint32_t hpos[16];
+    __shared__ uint64_t row_off[1 << kMaxSweepHigh];
+    __shared__ int s_fail;
     const uint32_t size = 1u << (g.L + g.H);
-    T *buf_r[2], *buf_i[2];
-    buf_r[0] = reinterpret_cast<T *>(smem);
-    buf_i[0] = buf_r[0] + size;
-    buf_r[1] = buf_i[0] + size;
-    buf_i[1] = buf_r[1] + size;
+    const uint32_t rows = 1u << g.H, row_elems = 1u << g.L, row_bytes = row_elems * (uint32_t)sizeof(T);
+    T *sre = reinterpret_cast<T *>(smem);
+    T *sim = sre + size;
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
     for (int i = tid; i < nops * (int)(sizeof(MicroOp) / 4); i += blockDim.x)
         reinterpret_cast<uint32_t *>(ops)[i] = reinterpret_cast<const uint32_t *>(gops)[i];
-    bool has_arith = false;
-    for (int o = 0; o < nops; o++) has_arith |= gops[o].kind == MOP_U1 || gops[o].kind == MOP_D1 || gops[o].kind == MOP_DK;
+    if (tid < 16) hpos[tid] = g.hpos[tid];
+    for (uint32_t r = tid; r < rows; r += blockDim.x) {
+        uint64_t o = 0;
+        for (uint32_t j = 0; j < g.H; j++) o |= (uint64_t)((r >> j) & 1) << g.hpos[j];
+        row_off[r] = o;
+    }
     if (tid == 0) {
-        mbar_init(&bars[0], 1);
-        mbar_init(&bars[1], 1);
+        s_fail = 0;
+        mbar_init(&bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
-    const uint64_t first = blockIdx.x, stride = gridDim.x;
-    // prefetch the first two tiles
-    if (warp == 0) {
-        for (int s = 0; s < 2; s++) {
-            const uint64_t t = first + s * stride;
-            if (t < g.ntiles) issue_tile_load(re, im, buf_r[s], buf_i[s], tile_base(t, g), g, &bars[s], lane);
+    bool has_arith = false;
+    for (int o = 0; o < nops; o++) has_arith |= ops[o].kind == MOP_U1 || ops[o].kind == MOP_D1 || ops[o].kind == MOP_DK;
+    if (tid < nops) {
+        const MicroOp &op = ops[tid];
+        if (op.kind == MOP_U1 || op.kind == MOP_D1) {
+            const int cnt = op.kind == MOP_U1 ? 8 : 4;
+            for (int i = 0; i < cnt; i++) {
+                if constexpr (A == AR_DF)
+                    coef[tid].v[i] = df_from_f64(op.m[i]);
+                else
+                    coef[tid].v[i] = (T)op.m[i];
+            }
         }
     }
-    __shared__ int s_fail;
-    if (tid == 0) s_fail = 0;
     __syncthreads();
-    uint32_t phase[2] = {0, 0};
-    int it = 0;
-    for (uint64_t t = first; t < g.ntiles; t += stride, it++) {
-        const int s = it & 1;
+    uint32_t phase = 0;
+    for (uint64_t t = blockIdx.x; t < g.ntiles; t += gridDim.x) {
+        const uint64_t base = tile_base(t, g.L, hpos, g.H);
+        if (warp == 0) {
+            if (lane == 0) mbar_expect_tx(&bar, 2u * rows * row_bytes);
+            __syncwarp();
+            for (uint32_t r = lane; r < rows; r += 32) {
+                const uint64_t gi = base | row_off[r];
+                bulk_load(sre + (size_t)r * row_elems, re + gi, row_bytes, &bar);
+                bulk_load(sim + (size_t)r * row_elems, im + gi, row_bytes, &bar);
+            }
+        }
         // Every thread waits; a timeout anywhere makes all threads leave together.
-        if (!mbar_wait(&bars[s], phase[s])) s_fail = 1;
+        if (!mbar_wait(&bar, phase)) s_fail = 1;
         __syncthreads();
         if (s_fail) break;
-        phase[s] ^= 1;
-        const uint64_t base = tile_base(t, g);
+        phase ^= 1;
         if constexpr (A == AR_DF) {
-            // f64 slots -> (hi, lo) pairs in place, double-float ops, back to f64
-            double *dr = reinterpret_cast<double *>(buf_r[s]), *di = reinterpret_cast<double *>(buf_i[s]);
-            float2 *fr = reinterpret_cast<float2 *>(dr), *fi = reinterpret_cast<float2 *>(di);
+            double *dr = reinterpret_cast<double *>(sre), *di = reinterpret_cast<double *>(sim);
+            float2 *fr = reinterpret_cast<float2 *>(sre), *fi = reinterpret_cast<float2 *>(sim);
             if (has_arith) {
                 for (uint32_t v = tid; v < size; v += blockDim.x) {
                     fr[v] = df_from_f64(dr[v]);
@@ -321,7 +276,7 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
                 }
                 __syncthreads();
             }
-            apply_ops_df(fr, fi, ops, nops, base, g, tables);
+            apply_ops<T, A, float2>(fr, fi, ops, coef, nops, base, size, tables);
             if (has_arith) {
                 for (uint32_t v = tid; v < size; v += blockDim.x) {
                     dr[v] = df_to_f64(fr[v]);
@@ -329,41 +284,41 @@ __global__ void __launch_bounds__(kSweepThreads, 1)
                 }
             }
         } else {
-            apply_ops<T, A>(buf_r[s], buf_i[s], ops, nops, base, g, tables);
+            apply_ops<T, A, T>(sre, sim, ops, coef, nops, base, size, tables);
         }
         fence_async_smem();
         __syncthreads();
         if (warp == 0) {
-            issue_tile_store(re, im, buf_r[s], buf_i[s], base, g, lane);
-            const uint64_t tn = t + 2 * stride;
-            if (tn < g.ntiles) {
-                bulk_wait_read_all();  // buffer s drained before it is refilled
-                issue_tile_load(re, im, buf_r[s], buf_i[s], tile_base(tn, g), g, &bars[s], lane);
+            for (uint32_t r = lane; r < rows; r += 32) {
+                const uint64_t gi = base | row_off[r];
+                bulk_store(re + gi, sre + (size_t)r * row_elems, row_bytes);
+                bulk_store(im + gi, sim + (size_t)r * row_elems, row_bytes);
             }
+            bulk_commit();
+            bulk_wait_read_all();  // the buffer is free once the stores have read it
         }
+        __syncthreads();
     }
-    if (s_fail) {
+    if (s_fail && tid == 0) {
         // Give the loads still in flight a bounded chance to land before exit.
-        if (tid == 0) {
-            mbar_wait(&bars[0], phase[0]);
-            mbar_wait(&bars[1], phase[1]);
-            atomicExch(err, 1);
-        }
+        mbar_wait(&bar, phase);
+        atomicExch(err, 1);
     }
     if (warp == 0) bulk_wait_all();
 }
 
 template <typename T, int A>
 int run_sweep(zc_state *st, const SweepGeom &g, const MicroOp *dev_ops, int nops, const char *dev_tables) {
-    const size_t smem = (size_t)4 * (1u << (g.L + g.H)) * sizeof(T);
+    const size_t smem = (size_t)2 * (1u << (g.L + g.H)) * sizeof(T);
     static bool attr = false;
     if (!attr) {
         ZC_CUDA(cudaFuncSetAttribute(k_sweep<T, A>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)kSweepSmemBytes));
         attr = true;
     }
-    if (smem > kSweepSmemBytes) return fail(ZC_ERR_INVALID, "sweep tile exceeds shared memory");
-    const uint64_t blocks = std::min<uint64_t>(g.ntiles, (uint64_t)st->num_sms);
+    if (smem > kSweepSmemBytes || g.H > kMaxSweepHigh || nops > kMaxMicroOps)
+        return fail(ZC_ERR_INVALID, "sweep shape exceeds the kernel's limits");
+    const uint64_t blocks = std::min<uint64_t>(g.ntiles, (uint64_t)st->num_sms * kSweepCtasPerSm);
     k_sweep<T, A><<<(int)blocks, kSweepThreads, smem, st->stream>>>((T *)st->re, (T *)st->im, g, dev_ops, nops,
                                                                        dev_tables, st->d_err);
     ZC_CUDA(cudaGetLastError());

@@ -6,8 +6,9 @@
 namespace zc {
 
 constexpr uint32_t kOuterFlag = 0x80000000u;  // operand names a non-local qubit (global position)
-constexpr int kMaxMicroOps = 48;               // ops per sweep
-constexpr size_t kSweepSmemBytes = 200 * 1024;
+constexpr int kMaxMicroOps = 32;               // ops per sweep
+constexpr uint32_t kMaxSweepHigh = 7;          // chosen high qubits per tile
+constexpr size_t kSweepSmemBytes = 64 * 1024;  // one tile buffer: 2^12 f64 or 2^13 f32 (re + im)
 
 enum : uint32_t { MOP_U1 = 1, MOP_D1 = 2, MOP_DK = 3, MOP_CX = 4, MOP_SWAP = 5 };
 

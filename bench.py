@@ -52,6 +52,7 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-check", action="store_true", help="skip the fast-vs-exact accuracy check")
     ap.add_argument("--check-qubits", type=int, default=26)
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched-trajectory measurement")
     return ap.parse_args()
 
 
@@ -85,6 +86,27 @@ def accuracy_check(a, zc, C):
     return {"qubits": a.check_qubits, "depth": a.depth, "max_abs_damp": d, "tvd": tvd,
             "reference": "exact mode (bit-identical to the FP64 oracle in the parity tests)",
             "tolerance": {"max_abs_damp": 1e-12 if a.precision == 64 else 1e-5, "tvd": 1e-6}}
+
+
+def batched_trajectories(zc, C):
+    """16 qubits, depth 20, depolarizing 1e-3 (1q) / 1e-2 (CX), damping 1e-3,
+    2% readout, 4096 trajectories in one launch vs the per-shot replay."""
+    noise = zc.NoiseModel(depolarizing_1q=1e-3, depolarizing_2q=1e-2, amplitude_damping=1e-3,
+                          readout_flip_0to1=0.02, readout_flip_1to0=0.02)
+    p = C.matching_circuit(16, 20, 7).to_program()
+    prog = zc.compile(p, 0)
+    zc.run(p, shots=256, seed=1, precision=32, noise=noise, program=prog)
+    t0 = time.perf_counter()
+    r = zc.run(p, shots=4096, seed=2, precision=32, noise=noise, program=prog)
+    tb = time.perf_counter() - t0
+    plain_shots = 32
+    t0 = time.perf_counter()
+    zc.run(p, shots=plain_shots, seed=2, precision=32, noise=noise, program=prog, flags=zc.FLAG_PER_SHOT)
+    tp = (time.perf_counter() - t0) / plain_shots
+    return {"workload": "16q depth-20 u3+matching-CX f32, dep 1e-3/1e-2, damping 1e-3, readout 2%, 4096 trajectories",
+            "trajectories_per_s": 4096 / tb, "seconds": tb, "launches": r.launches, "batched": r.batched,
+            "plain_per_shot_trajectories_per_s": 1.0 / tp, "plain_sample_shots": plain_shots,
+            "speedup_vs_plain": (4096 / tb) * tp}
 
 
 class Clocks:
@@ -135,24 +157,6 @@ class Clocks:
         reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower().startswith("active")})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(rows)}
-
-
-def op_class(op, zc):
-    if op.kind == zc.OP_UNITARY:
-        return "1q" if len(op.qubits) == 1 else "kq%d" % len(op.qubits)
-    if op.kind == zc.OP_DIAG:
-        return "diag"
-    if op.kind == zc.OP_CX:
-        return "cx"
-    if op.kind == zc.OP_SWAP:
-        return "swap"
-    return "other"
-
-
-def op_bytes(op, zc, state_bytes):
-    """Algorithmic HBM bytes of one op: a full pass reads and writes the state
-    (2S); CX / SWAP move only the half that changes (S)."""
-    return state_bytes if op.kind in (zc.OP_CX, zc.OP_SWAP) else 2 * state_bytes
 
 
 def cpu_baseline(a, threads=None):
@@ -257,11 +261,9 @@ def main():
     S = (1 << a.qubits) * (a.precision // 8) * 2
     sample_seed = splitmix64(a.seed)
 
-    def step(events=None):
+    def step():
         be.reset_all()
-        if events is not None:
-            events[0].record(stream)
-        for i, op in enumerate(ops):
+        for op in ops:
             if op.kind == zc.OP_UNITARY:
                 be.apply_unitary(op.qubits, op.data)
             elif op.kind == zc.OP_DIAG:
@@ -270,24 +272,22 @@ def main():
                 be.apply_cx(op.a, op.b)
             elif op.kind == zc.OP_SWAP:
                 be.apply_swap(op.a, op.b)
-            if events is not None:
-                events[i + 1].record(stream)
         return be.sample(a.shots, sample_seed)
 
     for _ in range(a.warmup):
         step()
     be.finish()
     c0 = be.counters()
-    evs = [[torch.cuda.Event(enable_timing=True) for _ in range(len(ops) + 1)] for _ in range(a.steps)]
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
+    be.profile(True)  # CUDA events around every launch, on the backend's stream
     with Clocks(dev) as clk:
         t_start = torch.cuda.Event(enable_timing=True)
         t_end = torch.cuda.Event(enable_timing=True)
         t_start.record(stream)
         for k in range(a.steps):
-            step(evs[k])
+            step()
         t_end.record(stream)
         be.finish()
         torch.cuda.synchronize()
@@ -295,21 +295,13 @@ def main():
         torch.distributed.barrier()
     elapsed = t_start.elapsed_time(t_end) / 1000.0
     c1 = be.counters()
+    classes = be.profile_read()
+    be.profile(False)
     if ws > 1:
         t = torch.tensor([elapsed], device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         elapsed = float(t.item())
-    # per-kernel-class durations from the per-op events
-    classes = {}
-    for k in range(a.steps):
-        for i, op in enumerate(ops):
-            c = op_class(op, zc)
-            ms = evs[k][i].elapsed_time(evs[k][i + 1])
-            d = classes.setdefault(c, {"launches": 0, "ms": 0.0, "bytes": 0})
-            d["launches"] += 1
-            d["ms"] += ms
-            d["bytes"] += op_bytes(op, zc, S)
-    gates_ms = sum(d["ms"] for d in classes.values())
+    gates_ms = sum(d["ms"] for d in classes.values())  # all of our kernels in the timed region
     dom = max(classes, key=lambda c: classes[c]["ms"])
     dd = classes[dom]
     peak, peak_kind = peaks()
@@ -325,8 +317,10 @@ def main():
                    "l2": "state %.0f GiB > 129 MB L2: no flush needed" % (S / 2**30),
                    "ops": len(ops), "input_gates": prog.stats["input_gates"]},
         "gpu_launches": int(c1["launches"] - c0["launches"]),
+        "gpu_busy_frac": gates_ms / 1000.0 / elapsed,
         "kernels": {c: {"launches": d["launches"], "avg_ms": d["ms"] / d["launches"],
-                        "GBps": (d["bytes"] / d["launches"]) / (d["ms"] / d["launches"] / 1000.0) / 1e9,
+                        "GBps": (d["bytes"] / d["launches"]) / (d["ms"] / d["launches"] / 1000.0) / 1e9
+                        if d["bytes"] else None,
                         "share": d["ms"] / gates_ms} for c, d in sorted(classes.items())},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
@@ -351,6 +345,8 @@ def main():
         line["e2e"] = {"value": 1.0 / statistics.median(ts), "unit": "circuits/s", "h2d_bytes_per_step": h2d,
                        "d2h_bytes_per_step": d2h, "sim_seconds": r.sim_time,
                        "path": "zc_run: allocate state, per-op host->device tables, kernels, sample, read indices"}
+    if rank == 0 and not a.no_extras:
+        line["batched_trajectories"] = batched_trajectories(zc, C)
     if rank == 0 and a.mode == "fast" and not a.no_check:
         line["accuracy"] = accuracy_check(a, zc, C)
     if rank == 0 and not a.no_cpu:

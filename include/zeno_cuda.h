@@ -34,6 +34,7 @@ extern "C" {
 #define ZC_FLAG_FAST 1u       /* FMA-contracted arithmetic (tolerance parity, not bit-exact) */
 #define ZC_FLAG_NO_SWEEPS 2u  /* one launch per op: disables multi-op sweep scheduling */
 #define ZC_FLAG_FORCE_SWEEPS 4u /* schedule sweeps even for small states (testing) */
+#define ZC_FLAG_PER_SHOT 8u   /* noisy runs: replay shot by shot (zeno's order and RNG) instead of batching */
 
 typedef struct zc_state zc_state;
 
@@ -104,6 +105,20 @@ typedef struct {
     uint64_t bytes_moved;    /* algorithmic HBM bytes of those passes */
 } zc_counters;
 int zc_get_counters(zc_state *st, zc_counters *out);
+
+/* Per-launch profiling: with profiling on, every kernel launch of this
+ * state is bracketed by CUDA events on its stream. zc_profile(st, 1)
+ * starts (and clears) a recording, zc_profile_read flushes, synchronises
+ * and returns one entry per kernel class that ran: launches, total time
+ * and the algorithmic HBM bytes those launches move. */
+typedef struct {
+    char name[24];
+    uint64_t launches;
+    double ms;
+    double bytes;
+} zc_kernel_stat;
+int zc_profile(zc_state *st, int enable);
+int zc_profile_read(zc_state *st, zc_kernel_stat *out, int cap, int *n);
 
 /* ------------------------------------------------------------------ *
  * Host pipeline: compiler and executor above the backend. These mirror *
@@ -190,6 +205,7 @@ typedef struct {
 
 typedef struct {
     int precision_bits;
+    int batched;           /* 1: noisy shots ran in the batched trajectory engine */
     uint64_t n_keys;       /* distinct clbit words (keys[] filled up to cap) */
     double sim_seconds;    /* state allocation + gates + sampling (src/exec.rs:372-381) */
     uint64_t launches;
@@ -200,7 +216,16 @@ typedef struct {
 /* Run a compiled program. Counts are returned as (clbit word, count)
  * pairs sorted by clbit word; format keys with the program's cregs
  * (exec::format_key, src/exec.rs:235-253). `statevector` (2^n c64) may be
- * NULL; it is rejected for dynamic or noisy programs. */
+ * NULL; it is rejected for dynamic or noisy programs.
+ *
+ * Noisy static programs at precision 32 run in the batched trajectory
+ * engine (no counterpart in zeno, which replays shots one by one,
+ * src/exec.rs:459-549): every shot is a trajectory with its own
+ * Philox4x32-10 stream (key = seed, counter = (draw, shot)), all in one
+ * launch; the channel order of src/noise.rs:145-175 is kept, results agree
+ * with zeno's per-shot path in distribution. ZC_FLAG_PER_SHOT (or f64, or a
+ * dynamic program) selects the per-shot replay, which reproduces zeno's RNG
+ * stream layout. */
 int zc_run(const zc_program *p, const zc_run_options *opt, zc_run_result *res, uint64_t *keys, uint64_t *counts,
            size_t cap, double *statevector);
 

@@ -22,7 +22,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libzeno_cuda.so")
 
 ZC_OK, ZC_ERR_INVALID, ZC_ERR_MEMORY, ZC_ERR_CUDA, ZC_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
-FLAG_EXACT, FLAG_FAST, FLAG_NO_SWEEPS, FLAG_FORCE_SWEEPS = 0, 1, 2, 4
+FLAG_EXACT, FLAG_FAST, FLAG_NO_SWEEPS, FLAG_FORCE_SWEEPS, FLAG_PER_SHOT = 0, 1, 2, 4, 8
 OP_UNITARY, OP_DIAG, OP_CX, OP_MEASURE, OP_RESET, OP_SWAP = 0, 1, 2, 3, 4, 6
 
 # Every entry point the header declares; the CPU test suite checks exports.
@@ -31,7 +31,8 @@ EXPORTS = (
     "zc_apply_cx", "zc_apply_swap", "zc_prob_one", "zc_measure", "zc_reset_all", "zc_sample",
     "zc_statevector", "zc_norm_sqr", "zc_finish", "zc_last_error", "zc_device_budget", "zc_state_bytes",
     "zc_max_qubits", "zc_load_state", "zc_get_stream", "zc_get_counters", "zc_compile", "zc_program_free",
-    "zc_program_get_info", "zc_program_get_op", "zc_program_get_final", "zc_run",
+    "zc_program_get_info", "zc_program_get_op", "zc_program_get_final", "zc_run", "zc_profile",
+    "zc_profile_read",
 )
 
 
@@ -43,6 +44,10 @@ class ZenoCudaError(RuntimeError):
 
 class Counters(C.Structure):
     _fields_ = [("ops", C.c_uint64), ("launches", C.c_uint64), ("sweeps", C.c_uint64), ("bytes_moved", C.c_uint64)]
+
+
+class KernelStat(C.Structure):
+    _fields_ = [("name", C.c_char * 24), ("launches", C.c_uint64), ("ms", C.c_double), ("bytes", C.c_double)]
 
 
 class Instr(C.Structure):
@@ -85,7 +90,7 @@ class RunOptions(C.Structure):
 
 
 class RunResultC(C.Structure):
-    _fields_ = [("precision_bits", C.c_int), ("n_keys", C.c_uint64), ("sim_seconds", C.c_double),
+    _fields_ = [("precision_bits", C.c_int), ("batched", C.c_int), ("n_keys", C.c_uint64), ("sim_seconds", C.c_double),
                 ("launches", C.c_uint64), ("sweeps", C.c_uint64), ("bytes_moved", C.c_uint64)]
 
 
@@ -153,6 +158,8 @@ def load() -> C.CDLL:
         "zc_program_get_op": ([vp, C.c_size_t, P(OpView)], i32),
         "zc_program_get_final": ([vp, C.c_size_t, P(u32), P(u32)], i32),
         "zc_run": ([vp, P(RunOptions), P(RunResultC), P(u64), P(u64), C.c_size_t, P(dbl)], i32),
+        "zc_profile": ([vp, i32], i32),
+        "zc_profile_read": ([vp, P(KernelStat), i32, P(i32)], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -251,6 +258,18 @@ class CudaBackend:
         c = Counters()
         _check(load().zc_get_counters(self._h, C.byref(c)))
         return {f: getattr(c, f) for f, _ in Counters._fields_}
+
+    def profile(self, enable: bool = True) -> None:
+        """Start (and clear) or stop per-launch CUDA-event recording."""
+        _check(load().zc_profile(self._h, 1 if enable else 0))
+
+    def profile_read(self) -> Dict[str, Dict[str, float]]:
+        """Per kernel class: launches, total ms, algorithmic bytes (flushes and syncs)."""
+        arr = (KernelStat * 32)()
+        n = C.c_int()
+        _check(load().zc_profile_read(self._h, arr, 32, C.byref(n)))
+        return {arr[i].name.decode(): {"launches": arr[i].launches, "ms": arr[i].ms, "bytes": arr[i].bytes}
+                for i in range(min(n.value, 32))}
 
     def close(self) -> None:
         if getattr(self, "_h", None):
@@ -371,6 +390,7 @@ class RunResult:
     launches: int
     sweeps: int
     bytes_moved: int
+    batched: bool = False
 
 
 def run(p, shots: int = 1024, seed: int = 0, precision: int = 0, fusion: Optional[int] = None,
@@ -404,7 +424,7 @@ def run(p, shots: int = 1024, seed: int = 0, precision: int = 0, fusion: Optiona
         fmt[key] = fmt.get(key, 0) + v
     prec = res.precision_bits
     return RunResult(fmt, raw, shots, p.n_qubits, prec, "cuda-f%d" % prec, seed, res.sim_seconds, sv,
-                     program.stats, res.launches, res.sweeps, res.bytes_moved)
+                     program.stats, res.launches, res.sweeps, res.bytes_moved, bool(res.batched))
 
 
 def device_budget(fraction: float = 0.75) -> int:

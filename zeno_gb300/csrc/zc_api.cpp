@@ -19,6 +19,30 @@ namespace zc {
 
 static thread_local std::string g_err;
 
+const char *const kKernelNames[K_NKINDS] = {"1q",         "kq",         "diag1",       "diagk",    "cx",
+                                            "swap",       "sweep",      "chunk_sums",  "serial_sum", "sample_scan",
+                                            "collapse",   "reset",      "trajectories"};
+
+ProfScope::ProfScope(zc_state *s, int kind, double bytes) : st(s) {
+    if (!st || !st->prof) return;
+    cudaEvent_t ev[2];
+    for (int i = 0; i < 2; i++) {
+        if (!st->prof_pool.empty()) {
+            ev[i] = st->prof_pool.back();
+            st->prof_pool.pop_back();
+        } else if (cudaEventCreate(&ev[i]) != cudaSuccess) {
+            return;
+        }
+    }
+    cudaEventRecord(ev[0], st->stream);
+    st->prof_recs.push_back(ProfRec{kind, bytes, ev[0], ev[1]});
+    idx = (long)st->prof_recs.size() - 1;
+}
+
+ProfScope::~ProfScope() {
+    if (idx >= 0) cudaEventRecord(st->prof_recs[idx].b, st->stream);
+}
+
 int fail(int code, const std::string &msg) {
     g_err = msg;
     return code;
@@ -459,6 +483,11 @@ void zc_destroy(zc_state *st) {
     if (st->h_scalar) cudaFreeHost(st->h_scalar);
     if (st->d_samp) cudaFree(st->d_samp);
     if (st->d_err) cudaFree(st->d_err);
+    for (auto &r : st->prof_recs) {
+        cudaEventDestroy(r.a);
+        cudaEventDestroy(r.b);
+    }
+    for (auto e : st->prof_pool) cudaEventDestroy(e);
     if (st->stream) cudaStreamDestroy(st->stream);
     delete st;
 }
@@ -642,6 +671,44 @@ int zc_finish(zc_state *st) {
 int zc_get_stream(zc_state *st, void **stream) {
     if (!st || !stream) return fail(ZC_ERR_INVALID, "null argument");
     *stream = (void *)st->stream;
+    return ZC_OK;
+}
+
+int zc_profile(zc_state *st, int enable) {
+    if (!st) return fail(ZC_ERR_INVALID, "null state");
+    for (auto &r : st->prof_recs) {
+        st->prof_pool.push_back(r.a);
+        st->prof_pool.push_back(r.b);
+    }
+    st->prof_recs.clear();
+    st->prof = enable != 0;
+    return ZC_OK;
+}
+
+int zc_profile_read(zc_state *st, zc_kernel_stat *out, int cap, int *n) {
+    if (!st || !n) return fail(ZC_ERR_INVALID, "null argument");
+    int rc = flush(st);
+    if (rc) return rc;
+    ZC_CUDA(cudaStreamSynchronize(st->stream));
+    zc_kernel_stat agg[K_NKINDS];
+    memset(agg, 0, sizeof agg);
+    for (const auto &r : st->prof_recs) {
+        float ms = 0.f;
+        ZC_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+        agg[r.kind].launches++;
+        agg[r.kind].ms += ms;
+        agg[r.kind].bytes += r.bytes;
+    }
+    int m = 0;
+    for (int k = 0; k < K_NKINDS; k++) {
+        if (!agg[k].launches) continue;
+        if (m < cap && out) {
+            out[m] = agg[k];
+            snprintf(out[m].name, sizeof out[m].name, "%s", kKernelNames[k]);
+        }
+        m++;
+    }
+    *n = m;
     return ZC_OK;
 }
 

@@ -403,6 +403,7 @@ __global__ void k_set_one(T *re) {
 }  // namespace
 
 int launch_1q(zc_state *st, uint32_t q, const double *m8, bool exact) {
+    ProfScope ps(st, K_1Q, 2.0 * st->len * (st->prec / 8) * 2);
     st->ctr.launches++;
     st->ctr.sweeps++;
     st->ctr.bytes_moved += 2 * st->len * (st->prec / 8) * 2;
@@ -411,6 +412,7 @@ int launch_1q(zc_state *st, uint32_t q, const double *m8, bool exact) {
 }
 
 int launch_kq(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat, bool exact) {
+    ProfScope ps(st, K_KQ, 2.0 * st->len * (st->prec / 8) * 2);
     st->ctr.launches++;
     st->ctr.sweeps++;
     st->ctr.bytes_moved += 2 * st->len * (st->prec / 8) * 2;
@@ -420,6 +422,7 @@ int launch_kq(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat,
 }
 
 int launch_diag1(zc_state *st, uint32_t q, const double *d4, bool exact) {
+    ProfScope ps(st, K_DIAG1, 2.0 * st->len * (st->prec / 8) * 2);
     st->ctr.launches++;
     st->ctr.sweeps++;
     st->ctr.bytes_moved += 2 * st->len * (st->prec / 8) * 2;
@@ -428,6 +431,7 @@ int launch_diag1(zc_state *st, uint32_t q, const double *d4, bool exact) {
 }
 
 int launch_diagk(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_diag, bool exact) {
+    ProfScope ps(st, K_DIAGK, 2.0 * st->len * (st->prec / 8) * 2);
     st->ctr.launches++;
     st->ctr.sweeps++;
     st->ctr.bytes_moved += 2 * st->len * (st->prec / 8) * 2;
@@ -437,6 +441,7 @@ int launch_diagk(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_d
 }
 
 int launch_cx(zc_state *st, uint32_t c, uint32_t t) {
+    ProfScope ps(st, K_CX, 1.0 * st->len * (st->prec / 8) * 2);
     st->ctr.launches++;
     st->ctr.sweeps++;
     st->ctr.bytes_moved += st->len * (st->prec / 8) * 2;  // half the amplitudes, read + write
@@ -446,6 +451,7 @@ int launch_cx(zc_state *st, uint32_t c, uint32_t t) {
 }
 
 int launch_swap(zc_state *st, uint32_t a, uint32_t b) {
+    ProfScope ps(st, K_SWAP, 1.0 * st->len * (st->prec / 8) * 2);
     st->ctr.launches++;
     st->ctr.sweeps++;
     st->ctr.bytes_moved += st->len * (st->prec / 8) * 2;
@@ -455,6 +461,7 @@ int launch_swap(zc_state *st, uint32_t a, uint32_t b) {
 }
 
 int launch_collapse(zc_state *st, uint32_t q, int outcome, double scale64) {
+    ProfScope ps(st, K_COLLAPSE, 2.0 * st->len * (st->prec / 8) * 2);
     st->ctr.launches++;
     const uint64_t half = st->len / 2;
     Launch L = grid_for(st, half);
@@ -469,6 +476,7 @@ int launch_collapse(zc_state *st, uint32_t q, int outcome, double scale64) {
 }
 
 int launch_reset(zc_state *st) {
+    ProfScope ps(st, K_RESET, 1.0 * st->len * (st->prec / 8) * 2);
     st->ctr.launches++;
     const size_t bytes = st->len * (st->prec / 8);
     ZC_CUDA(cudaMemsetAsync(st->re, 0, bytes, st->stream));

@@ -19,6 +19,7 @@
 
 #include "zc_internal.h"
 #include "zc_rng.h"
+#include "zc_traj.h"
 
 namespace zc {
 namespace {
@@ -644,6 +645,88 @@ void histogram(std::vector<uint64_t> &w, std::vector<std::pair<uint64_t, uint64_
     }
 }
 
+// Can the batched trajectory engine run this noisy program?
+bool batchable(const zc_program *p) {
+    if (p->dynamic) return false;
+    for (const Op &o : p->ops) {
+        if (!o.gate_like()) return false;
+        if ((o.kind == ZC_OP_UNITARY || o.kind == ZC_OP_DIAG) && o.qs.size() > 3) return false;
+    }
+    return true;
+}
+
+// Noisy static program, all shots as trajectories in one launch.
+int run_batched(const zc_program *p, const zc_run_options *opt, const zc_noise &nz,
+                std::vector<std::pair<uint64_t, uint64_t>> *hist, zc_run_result *res) {
+    std::vector<TrajOp> tops;
+    std::vector<double> mats;
+    for (const Op &o : p->ops) {
+        std::vector<uint32_t> sup;
+        Mat m = dense_of(o, &sup);
+        TrajOp t{};
+        t.k = (uint32_t)sup.size();
+        for (size_t i = 0; i < sup.size(); i++) t.qs[i] = sup[i];
+        t.mat_off = (uint32_t)mats.size();
+        for (const Cx &c : m) {
+            mats.push_back(c.re);
+            mats.push_back(c.im);
+        }
+        tops.push_back(t);
+    }
+    std::vector<uint32_t> fq, fc;
+    for (const auto &f : p->finals) {
+        fq.push_back(f.first);
+        fc.push_back(f.second);
+    }
+    TrajNoise tn{{nz.depolarizing_1q, nz.depolarizing_2q, nz.bit_flip, nz.phase_flip, nz.amplitude_damping,
+                  nz.readout_flip_0to1, nz.readout_flip_1to0}};
+    zc_state *ctx = nullptr;
+    int rc = zc_create_ex(1, 32, opt->flags, &ctx);
+    if (rc) return rc;
+    const uint64_t ntraj = opt->shots;
+    const size_t per_cta = ((size_t)2 << p->n_qubits) * sizeof(float);
+    uint64_t budget = 0;
+    zc_device_budget(opt->mem_fraction > 0 ? opt->mem_fraction : 0.75, &budget);
+    uint64_t ctas = std::min<uint64_t>(ntraj, (uint64_t)ctx->num_sms * 2);
+    ctas = std::min<uint64_t>(ctas, std::max<uint64_t>(1, budget / std::max<size_t>(per_cta, 1)));
+    void *d_work = nullptr, *d_buf = nullptr;
+    const size_t ops_b = tops.size() * sizeof(TrajOp), mats_b = mats.size() * sizeof(double);
+    const size_t f_b = (fq.size() + 1) * sizeof(uint32_t), out_b = ntraj * sizeof(uint64_t);
+    const size_t off_mats = (ops_b + 255) & ~(size_t)255, off_fq = off_mats + ((mats_b + 255) & ~(size_t)255);
+    const size_t off_fc = off_fq + ((f_b + 255) & ~(size_t)255), off_out = off_fc + ((f_b + 255) & ~(size_t)255);
+    std::vector<uint64_t> words(ntraj);
+    auto cleanup = [&](int code) {
+        if (d_work) cudaFree(d_work);
+        if (d_buf) cudaFree(d_buf);
+        zc_counters c{};
+        zc_get_counters(ctx, &c);
+        res->launches = c.launches;
+        zc_destroy(ctx);
+        return code;
+    };
+    cudaError_t e = cudaMalloc(&d_work, per_cta * ctas);
+    if (e == cudaSuccess) e = cudaMalloc(&d_buf, off_out + out_b);
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "cudaMalloc (trajectory buffers)"));
+    char *b = (char *)d_buf;
+    cudaStream_t s = ctx->stream;
+    if (!tops.empty()) cudaMemcpyAsync(b, tops.data(), ops_b, cudaMemcpyHostToDevice, s);
+    if (!mats.empty()) cudaMemcpyAsync(b + off_mats, mats.data(), mats_b, cudaMemcpyHostToDevice, s);
+    if (!fq.empty()) {
+        cudaMemcpyAsync(b + off_fq, fq.data(), fq.size() * 4, cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(b + off_fc, fc.data(), fc.size() * 4, cudaMemcpyHostToDevice, s);
+    }
+    rc = launch_trajectories(ctx, p->n_qubits, (const TrajOp *)b, (int)tops.size(), (const double *)(b + off_mats),
+                             (const uint32_t *)(b + off_fq), (const uint32_t *)(b + off_fc), (int)fq.size(), tn, ntraj,
+                             opt->seed, (uint64_t *)(b + off_out), d_work, (int)ctas);
+    if (rc) return cleanup(rc);
+    e = cudaMemcpyAsync(words.data(), b + off_out, out_b, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cleanup(cuda_fail(e, "trajectory launch"));
+    histogram(words, hist);
+    res->batched = 1;
+    return cleanup(ZC_OK);
+}
+
 }  // namespace
 }  // namespace zc
 
@@ -747,6 +830,17 @@ int zc_run(const zc_program *p, const zc_run_options *opt, zc_run_result *res, u
     if (prec == 0) prec = zc_state_bytes(p->n_qubits, 64) <= budget ? 64 : 32;
     res->precision_bits = prec;
     const auto t0 = std::chrono::steady_clock::now();
+    if (noise && prec == 32 && !(opt->flags & ZC_FLAG_PER_SHOT) && batchable(p)) {
+        std::vector<std::pair<uint64_t, uint64_t>> hist;
+        rc = p->finals.empty() ? ZC_OK : run_batched(p, opt, *noise, &hist, res);
+        res->sim_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        res->n_keys = hist.size();
+        for (size_t i = 0; i < hist.size() && i < cap; i++) {
+            keys[i] = hist[i].first;
+            counts[i] = hist[i].second;
+        }
+        return rc;
+    }
     zc_state *st = nullptr;
     rc = zc_create_ex(p->n_qubits, prec, opt->flags, &st);
     if (rc) return rc;

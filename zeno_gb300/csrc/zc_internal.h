@@ -40,6 +40,19 @@ struct Launch {
     int threads;
 };
 
+// Kernel classes for the per-launch profiler (zc_profile / zc_profile_read).
+enum : int {
+    K_1Q = 0, K_KQ, K_DIAG1, K_DIAGK, K_CX, K_SWAP, K_SWEEP, K_CHUNK_SUMS, K_SERIAL_SUM, K_SAMPLE_SCAN,
+    K_COLLAPSE, K_RESET, K_TRAJ, K_NKINDS
+};
+extern const char *const kKernelNames[K_NKINDS];
+
+struct ProfRec {
+    int kind;
+    double bytes;
+    cudaEvent_t a, b;
+};
+
 // An op accepted by the ABI and not yet launched.
 enum : int { Q_UNITARY = 0, Q_DIAG = 1, Q_CX = 2, Q_SWAP = 3 };
 struct QOp {
@@ -72,6 +85,9 @@ struct zc_state {
     size_t samp_cap = 0;
     int *d_err = nullptr;        // device error flag (sweep wait timeouts)
     std::vector<zc::QOp> queue;  // ops waiting to be scheduled into sweeps
+    bool prof = false;            // record CUDA events around every launch
+    std::vector<zc::ProfRec> prof_recs;
+    std::vector<cudaEvent_t> prof_pool;
     zc_counters ctr{};
     std::string name;
 };
@@ -80,6 +96,14 @@ namespace zc {
 
 // Kernel launchers (zc_gates.cu / zc_reduce.cu). All are asynchronous on
 // st->stream and return ZC_OK or an error code.
+// Records CUDA events around one launch on st->stream while profiling is on.
+struct ProfScope {
+    zc_state *st;
+    long idx = -1;
+    ProfScope(zc_state *s, int kind, double bytes);
+    ~ProfScope();
+};
+
 int launch_1q(zc_state *st, uint32_t q, const double *m8, bool exact);
 int launch_kq(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat, bool exact);
 int launch_diag1(zc_state *st, uint32_t q, const double *d4, bool exact);
@@ -104,6 +128,11 @@ struct SweepGeom;
 struct MicroOp;
 int launch_sweep(zc_state *st, const SweepGeom &g, const MicroOp *dev_ops, int nops, const char *dev_tables,
                  bool exact);
+struct TrajOp;
+struct TrajNoise;
+int launch_trajectories(zc_state *st, uint32_t n, const TrajOp *d_ops, int nops, const double *d_mats,
+                        const uint32_t *d_fq, const uint32_t *d_fc, int nfinal, const TrajNoise &nz, uint64_t ntraj,
+                        uint64_t seed, uint64_t *d_out, void *d_work, int ctas);
 int launch_sample_scan(zc_state *st, const SampleChunk *d_chunks, size_t nchunks, const double *d_us,
                        uint64_t *d_out, uint64_t chunk_len);
 

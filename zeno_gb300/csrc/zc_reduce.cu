@@ -116,6 +116,7 @@ int launch_chunk_sums(zc_state *st, int mode, uint32_t q, size_t *nchunks_out) {
     }
     const uint64_t per_block = kWarps * 32;
     const int blocks = (int)((nch + per_block - 1) / per_block);
+    ProfScope ps(st, K_CHUNK_SUMS, (mode == 0 ? 1.0 : 0.5) * st->len * (st->prec / 8) * 2);
     st->ctr.launches++;
     if (st->prec == 64)
         k_chunk_sums<double><<<blocks, kWarps * 32, 0, st->stream>>>((const double *)st->re, (const double *)st->im,
@@ -129,6 +130,7 @@ int launch_chunk_sums(zc_state *st, int mode, uint32_t q, size_t *nchunks_out) {
 }
 
 int launch_serial_sum(zc_state *st, size_t nchunks) {
+    ProfScope ps(st, K_SERIAL_SUM, 8.0 * nchunks);
     st->ctr.launches++;
     k_serial_sum<<<1, 1, 0, st->stream>>>(st->d_part, nchunks, st->d_scalar);
     ZC_CUDA(cudaGetLastError());
@@ -138,6 +140,7 @@ int launch_serial_sum(zc_state *st, size_t nchunks) {
 int launch_sample_scan(zc_state *st, const SampleChunk *d_chunks, size_t nchunks, const double *d_us,
                        uint64_t *d_out, uint64_t chunk_len) {
     if (nchunks == 0) return ZC_OK;
+    ProfScope ps(st, K_SAMPLE_SCAN, (double)nchunks * chunk_len * (st->prec / 8) * 2);
     st->ctr.launches++;
     const int threads = 128;
     const int blocks = (int)((nchunks + threads - 1) / threads);

@@ -329,6 +329,7 @@ int run_sweep(zc_state *st, const SweepGeom &g, const MicroOp *dev_ops, int nops
 
 int launch_sweep(zc_state *st, const SweepGeom &g, const MicroOp *dev_ops, int nops, const char *dev_tables,
                  bool exact) {
+    ProfScope ps(st, K_SWEEP, 2.0 * st->len * (st->prec / 8) * 2);
     st->ctr.launches++;
     st->ctr.sweeps++;
     st->ctr.bytes_moved += 2 * st->len * (st->prec / 8) * 2;

@@ -32,6 +32,12 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 HBM_FALLBACK_GBS = 6800.0
+# DRAM read+write per launch over algorithmic bytes, from an ncu capture of
+# the f64 double-float sweep kernel at 26 qubits (state 8x the L2):
+# 1.075 GB read + 1.023 GB write against 2S = 2.147 GB.
+MEASURED_TRAFFIC_RATIO = {"sweep": (1.075e9 + 1.023e9) / 2.147e9}
+# The same capture: issue slots 73% busy, FMA pipe 58%, FP64 pipe 0%.
+SWEEP_DF_PIPES = {"issue_active_pct": 73.0, "fma_pipe_pct": 58.0, "fp64_pipe_pct": 0.0}
 
 
 def parse():
@@ -324,7 +330,13 @@ def main():
                         "share": d["ms"] / gates_ms} for c, d in sorted(classes.items())},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
-                     "bytes_per_launch": dd["bytes"] / dd["launches"], "traffic": None},
+                     "bytes_per_launch": dd["bytes"] / dd["launches"],
+                     "traffic": (MEASURED_TRAFFIC_RATIO[dom] * dd["bytes"] / dd["launches"]
+                                 if dom in MEASURED_TRAFFIC_RATIO else None),
+                     "ops_per_launch": len(ops) * a.steps / dd["launches"] if dom == "sweep" else 1.0,
+                     "limiter": ("FP32/ALU issue: each sweep applies many gates per HBM pass in double-float "
+                                 "arithmetic; ncu at 26q: %s" % SWEEP_DF_PIPES)
+                     if dom == "sweep" and a.mode == "fast" and a.precision == 64 else None},
         "clocks": clk.summary(),
     }
     if not a.no_e2e:

@@ -10,19 +10,24 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
-def declared_symbols():
-    src = open(os.path.join(ROOT, "include", "zeno_cuda.h")).read()
+def declared_symbols(header):
+    src = open(os.path.join(ROOT, "include", header)).read()
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"\b(zc_[a-z0-9_]+)\s*\(", src)))
 
 
 def test_header_exports(zc):
+    from zeno_gb300 import serve
+
     lib = ctypes.CDLL(zc.LIB_PATH)
-    names = declared_symbols()
-    assert len(names) >= 25
-    missing = [n for n in names if not hasattr(lib, n)]
+    headers = sorted(f for f in os.listdir(os.path.join(ROOT, "include")) if f.endswith(".h"))
+    assert headers == ["zeno_cuda.h", "zeno_cuda_serve.h"]
+    core, srv = declared_symbols("zeno_cuda.h"), declared_symbols("zeno_cuda_serve.h")
+    assert len(core) >= 25 and len(srv) == 6
+    missing = [n for n in core + srv if not hasattr(lib, n)]
     assert not missing, missing
-    assert sorted(zc.EXPORTS) == names
+    assert sorted(zc.EXPORTS) == core
+    assert sorted(serve.EXPORTS) == srv
 
 
 def test_capacity_planning(zc):

@@ -71,7 +71,7 @@ static std::string human_bytes(double b) {
 static constexpr size_t kArenaBytes = 32u << 20;
 
 // Copy `bytes` into the device parameter ring and return its device address.
-static int arena_put(zc_state *st, const void *src, size_t bytes, const void **dev) {
+int arena_put(zc_state *st, const void *src, size_t bytes, const void **dev) {
     Arena &a = st->arena;
     const size_t need = (bytes + 255) & ~(size_t)255;
     if (need > a.cap) return fail(ZC_ERR_INVALID, "op table larger than the parameter arena");
@@ -142,7 +142,7 @@ static constexpr size_t kQueueWindow = 2048;  // ops examined per sweep plan
 static constexpr size_t kQueueFlushAt = 8192; // queue length that forces a flush
 static constexpr uint32_t kMinSweepQubits = 14;
 
-static int launch_single(zc_state *st, const QOp &op) {
+int launch_single(zc_state *st, const QOp &op) {
     const bool ex = exact(st);
     switch (op.kind) {
         case Q_UNITARY: {
@@ -208,16 +208,17 @@ static uint32_t loc_of(uint32_t q, uint32_t L, const std::vector<uint32_t> &high
     return kOuterFlag | q;
 }
 
-// Plan and launch one sweep starting at the queue front; erases what ran.
-static int run_one_sweep(zc_state *st) {
-    std::vector<QOp> &q = st->queue;
-    const SweepShape sh = shape_for(st);
-    const bool ex = exact(st);
-    const uint64_t low_mask = sh.L >= 64 ? ~0ull : ((1ull << sh.L) - 1);
+// Choose the ops of one sweep from the queue front (see the scheduling
+// rules above). Fills `plan` and returns how many ops it took; 0 or 1 means
+// the front op should simply run on its own.
+size_t plan_sweep(uint32_t n, int prec, bool ex, uint32_t L, uint32_t Hcap, const std::vector<QOp> &q,
+                  SweepPlan *plan) {
+    const uint64_t low_mask = L >= 64 ? ~0ull : ((1ull << L) - 1);
     uint64_t blocked = 0, highs_mask = 0;
     uint32_t nhigh = 0;
     bool arith_deferred = false;
-    std::vector<size_t> taken;
+    std::vector<size_t> &taken = plan->taken;
+    taken.clear();
     const size_t window = std::min(q.size(), kQueueWindow);
     for (size_t i = 0; i < window && taken.size() < (size_t)kMaxMicroOps; i++) {
         const QOp &op = q[i];
@@ -227,7 +228,7 @@ static int run_one_sweep(zc_state *st) {
         uint64_t need = 0;
         if (!defer) {
             need = need_mask(op) & ~low_mask & ~highs_mask;
-            if (nhigh + (uint32_t)__builtin_popcountll(need) > sh.Hcap) defer = true;
+            if (nhigh + (uint32_t)__builtin_popcountll(need) > Hcap) defer = true;
         }
         if (defer) {
             blocked |= touch;
@@ -238,35 +239,31 @@ static int run_one_sweep(zc_state *st) {
         nhigh += (uint32_t)__builtin_popcountll(need);
         taken.push_back(i);
     }
-    if (taken.size() <= 1) {
-        // nothing to batch: the per-op kernel is the same work
-        int rc = launch_single(st, q.front());
-        q.erase(q.begin());
-        return rc;
-    }
+    if (taken.size() <= 1) return taken.size();
     // pad the tile with further high qubits up to the cap (no effect on results)
-    for (uint32_t b = sh.L; b < st->n && nhigh < sh.Hcap; b++)
+    for (uint32_t b = L; b < n && nhigh < Hcap; b++)
         if (!((highs_mask >> b) & 1)) {
             highs_mask |= 1ull << b;
             nhigh++;
         }
     std::vector<uint32_t> highs;
-    for (uint32_t b = 0; b < st->n; b++)
+    for (uint32_t b = 0; b < n; b++)
         if ((highs_mask >> b) & 1) highs.push_back(b);
-    SweepGeom g{};
-    g.n = st->n;
-    g.L = sh.L;
+    SweepGeom &g = plan->g;
+    g = SweepGeom{};
+    g.n = n;
+    g.L = L;
     g.H = (uint32_t)highs.size();
     for (size_t j = 0; j < highs.size(); j++) g.hpos[j] = highs[j];
-    g.ntiles = 1ull << (st->n - g.L - g.H);
-    // encode: [MicroOp x nops][tables...]
-    std::vector<MicroOp> mops(taken.size());
-    std::vector<char> tables;
-    const size_t es = st->prec / 8;
+    g.ntiles = 1ull << (n - g.L - g.H);
+    std::vector<MicroOp> &mops = plan->mops;
+    std::vector<char> &tables = plan->tables;
+    mops.assign(taken.size(), MicroOp{});
+    tables.clear();
+    const size_t es = prec / 8;
     for (size_t t = 0; t < taken.size(); t++) {
         const QOp &op = q[taken[t]];
         MicroOp &m = mops[t];
-        memset(&m, 0, sizeof m);
         if (op.kind == Q_UNITARY) {
             m.kind = MOP_U1;
             m.a = loc_of(op.qs[0], g.L, highs);
@@ -302,16 +299,11 @@ static int run_one_sweep(zc_state *st) {
             m.b = loc_of(op.b, g.L, highs);
         }
     }
-    const size_t ops_bytes = mops.size() * sizeof(MicroOp);
-    const size_t tab_off = (ops_bytes + 255) & ~(size_t)255;
-    std::vector<char> blob(tab_off + tables.size());
-    memcpy(blob.data(), mops.data(), ops_bytes);
-    if (!tables.empty()) memcpy(blob.data() + tab_off, tables.data(), tables.size());
-    const void *dev = nullptr;
-    int rc = arena_put(st, blob.data(), blob.size(), &dev);
-    if (rc) return rc;
-    rc = launch_sweep(st, g, (const MicroOp *)dev, (int)mops.size(), (const char *)dev + tab_off, ex);
-    // drop the ops that ran (indices ascending)
+    return taken.size();
+}
+
+// Remove the ops at the (ascending) indices `taken`, keeping the rest in order.
+void erase_taken(std::vector<QOp> &q, const std::vector<size_t> &taken) {
     std::vector<QOp> rest;
     rest.reserve(q.size() - taken.size());
     size_t ti = 0;
@@ -323,6 +315,30 @@ static int run_one_sweep(zc_state *st) {
         rest.push_back(std::move(q[i]));
     }
     q.swap(rest);
+}
+
+// Plan and launch one sweep starting at the queue front; erases what ran.
+static int run_one_sweep(zc_state *st) {
+    std::vector<QOp> &q = st->queue;
+    const SweepShape sh = shape_for(st);
+    SweepPlan plan;
+    if (plan_sweep(st->n, st->prec, exact(st), sh.L, sh.Hcap, q, &plan) <= 1) {
+        // nothing to batch: the per-op kernel is the same work
+        int rc = launch_single(st, q.front());
+        q.erase(q.begin());
+        return rc;
+    }
+    const size_t ops_bytes = plan.mops.size() * sizeof(MicroOp);
+    const size_t tab_off = (ops_bytes + 255) & ~(size_t)255;
+    std::vector<char> blob(tab_off + plan.tables.size());
+    memcpy(blob.data(), plan.mops.data(), ops_bytes);
+    if (!plan.tables.empty()) memcpy(blob.data() + tab_off, plan.tables.data(), plan.tables.size());
+    const void *dev = nullptr;
+    int rc = arena_put(st, blob.data(), blob.size(), &dev);
+    if (rc) return rc;
+    rc = launch_sweep(st, plan.g, (const MicroOp *)dev, (int)plan.mops.size(), (const char *)dev + tab_off,
+                      exact(st));
+    erase_taken(q, plan.taken);
     return rc;
 }
 

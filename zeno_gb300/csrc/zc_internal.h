@@ -124,8 +124,23 @@ struct SampleChunk {
     uint64_t s0, s1; // draw range
     double cum;      // cum_before[chunk]
 };
-struct SweepGeom;
-struct MicroOp;
+}  // namespace zc
+#include "zc_sweep.h"
+namespace zc {
+// A planned sweep: tile geometry, encoded micro-ops, diagonal tables and the
+// queue indices it consumes.
+struct SweepPlan {
+    SweepGeom g;
+    std::vector<MicroOp> mops;
+    std::vector<char> tables;
+    std::vector<size_t> taken;
+};
+size_t plan_sweep(uint32_t n, int prec, bool ex, uint32_t L, uint32_t Hcap, const std::vector<QOp> &q,
+                  SweepPlan *plan);
+void erase_taken(std::vector<QOp> &q, const std::vector<size_t> &taken);
+int launch_single(zc_state *st, const QOp &op);
+int launch_sweep_multi(cudaStream_t stream, int num_sms, int prec, bool exact, const char *dev_blob, int *d_err);
+int arena_put(zc_state *st, const void *src, size_t bytes, const void **dev);
 int launch_sweep(zc_state *st, const SweepGeom &g, const MicroOp *dev_ops, int nops, const char *dev_tables,
                  bool exact);
 struct TrajOp;

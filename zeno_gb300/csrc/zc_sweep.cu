@@ -202,109 +202,191 @@ __device__ void apply_ops(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *
     }
 }
 
-// One CTA streams tiles through a single shared-memory buffer; three CTAs
-// per SM overlap one tile's TMA traffic with the others' arithmetic.
+// Per-CTA state of a sweep: the current job's micro-ops, coefficients and
+// row offsets, plus the tile buffer's mbarrier.
+template <typename T, int A>
+struct SweepSmem {
+    uint64_t bar;
+    MicroOp ops[kMaxMicroOps];
+    OpCoef<T, A> coef[kMaxMicroOps];
+    uint32_t hpos[16];
+    uint64_t row_off[1 << kMaxSweepHigh];
+    int nops;
+    uint32_t L, H;
+    int has_arith;
+    int fail;
+};
+
+// All threads: make (gops, nops, L, H, hpos) the CTA's current job.
+template <typename T, int A>
+__device__ void load_job(SweepSmem<T, A> &c, const MicroOp *gops, int nops, uint32_t L, uint32_t H,
+                         const uint32_t *hpos) {
+    const int tid = threadIdx.x;
+    __syncthreads();  // the previous job's tiles are done with the tables
+    for (int i = tid; i < nops * (int)(sizeof(MicroOp) / 4); i += blockDim.x)
+        reinterpret_cast<uint32_t *>(c.ops)[i] = reinterpret_cast<const uint32_t *>(gops)[i];
+    if (tid < 16) c.hpos[tid] = tid < (int)H ? hpos[tid] : 0u;
+    for (uint32_t r = tid; r < (1u << H); r += blockDim.x) {
+        uint64_t o = 0;
+        for (uint32_t j = 0; j < H; j++) o |= (uint64_t)((r >> j) & 1) << hpos[j];
+        c.row_off[r] = o;
+    }
+    if (tid == 0) {
+        c.nops = nops;
+        c.L = L;
+        c.H = H;
+    }
+    __syncthreads();
+    if (tid < nops) {
+        const MicroOp &op = c.ops[tid];
+        if (op.kind == MOP_U1 || op.kind == MOP_D1) {
+            const int cnt = op.kind == MOP_U1 ? 8 : 4;
+            for (int i = 0; i < cnt; i++) {
+                if constexpr (A == AR_DF)
+                    c.coef[tid].v[i] = df_from_f64(op.m[i]);
+                else
+                    c.coef[tid].v[i] = (T)op.m[i];
+            }
+        }
+    }
+    if (tid == 0) {
+        int ar = 0;
+        for (int o = 0; o < nops; o++) ar |= c.ops[o].kind == MOP_U1 || c.ops[o].kind == MOP_D1 || c.ops[o].kind == MOP_DK;
+        c.has_arith = ar;
+    }
+    __syncthreads();
+}
+
+// All threads: one tile of the current job — TMA row loads, micro-ops in
+// shared memory, TMA row stores. Returns false if a wait ran out.
+template <typename T, int A>
+__device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const char *tables, T *sre, T *sim,
+                             uint32_t &phase) {
+    const uint32_t size = 1u << (c.L + c.H);
+    const uint32_t rows = 1u << c.H, row_elems = 1u << c.L, row_bytes = row_elems * (uint32_t)sizeof(T);
+    const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
+    const uint64_t base = tile_base(t, c.L, c.hpos, c.H);
+    if (warp == 0) {
+        if (lane == 0) mbar_expect_tx(&c.bar, 2u * rows * row_bytes);
+        __syncwarp();
+        for (uint32_t r = lane; r < rows; r += 32) {
+            const uint64_t gi = base | c.row_off[r];
+            bulk_load(sre + (size_t)r * row_elems, re + gi, row_bytes, &c.bar);
+            bulk_load(sim + (size_t)r * row_elems, im + gi, row_bytes, &c.bar);
+        }
+    }
+    // Every thread waits; a timeout anywhere makes all threads leave together.
+    if (!mbar_wait(&c.bar, phase)) c.fail = 1;
+    __syncthreads();
+    if (c.fail) return false;
+    phase ^= 1;
+    if constexpr (A == AR_DF) {
+        double *dr = reinterpret_cast<double *>(sre), *di = reinterpret_cast<double *>(sim);
+        float2 *fr = reinterpret_cast<float2 *>(sre), *fi = reinterpret_cast<float2 *>(sim);
+        if (c.has_arith) {
+            for (uint32_t v = tid; v < size; v += blockDim.x) {
+                fr[v] = df_from_f64(dr[v]);
+                fi[v] = df_from_f64(di[v]);
+            }
+            __syncthreads();
+        }
+        apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables);
+        if (c.has_arith) {
+            for (uint32_t v = tid; v < size; v += blockDim.x) {
+                dr[v] = df_to_f64(fr[v]);
+                di[v] = df_to_f64(fi[v]);
+            }
+        }
+    } else {
+        apply_ops<T, A, T>(sre, sim, c.ops, c.coef, c.nops, base, size, tables);
+    }
+    fence_async_smem();
+    __syncthreads();
+    if (warp == 0) {
+        for (uint32_t r = lane; r < rows; r += 32) {
+            const uint64_t gi = base | c.row_off[r];
+            bulk_store(re + gi, sre + (size_t)r * row_elems, row_bytes);
+            bulk_store(im + gi, sim + (size_t)r * row_elems, row_bytes);
+        }
+        bulk_commit();
+        bulk_wait_read_all();  // the buffer is free once the stores have read it
+    }
+    __syncthreads();
+    return true;
+}
+
+template <typename T, int A>
+__device__ void sweep_init(SweepSmem<T, A> &c) {
+    if (threadIdx.x == 0) {
+        c.fail = 0;
+        mbar_init(&c.bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+}
+
+template <typename T, int A>
+__device__ void sweep_exit(SweepSmem<T, A> &c, uint32_t phase, int *err) {
+    if (c.fail && threadIdx.x == 0) {
+        // Give the loads still in flight a bounded chance to land before exit.
+        mbar_wait(&c.bar, phase);
+        atomicExch(err, 1);
+    }
+    if (threadIdx.x / 32 == 0) bulk_wait_all();
+}
+
+// One state. One CTA streams tiles through a single shared-memory buffer;
+// three CTAs per SM overlap one tile's TMA traffic with the others' arithmetic.
 template <typename T, int A>
 __global__ void __launch_bounds__(kSweepThreads, kSweepCtasPerSm)
     k_sweep(T *__restrict__ re, T *__restrict__ im, const SweepGeom g, const MicroOp *__restrict__ gops, int nops,
             const char *__restrict__ tables, int *__restrict__ err) {
     extern __shared__ __align__(1024) unsigned char smem[];
-    __shared__ __align__(8) uint64_t bar;
-    __shared__ MicroOp ops[kMaxMicroOps];
-    __shared__ OpCoef<T, A> coef[kMaxMicroOps];
-    __shared__ uint32_t hpos[16];
-    __shared__ uint64_t row_off[1 << kMaxSweepHigh];
-    __shared__ int s_fail;
-    const uint32_t size = 1u << (g.L + g.H);
-    const uint32_t rows = 1u << g.H, row_elems = 1u << g.L, row_bytes = row_elems * (uint32_t)sizeof(T);
+    __shared__ SweepSmem<T, A> c;
     T *sre = reinterpret_cast<T *>(smem);
-    T *sim = sre + size;
-    const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
-    for (int i = tid; i < nops * (int)(sizeof(MicroOp) / 4); i += blockDim.x)
-        reinterpret_cast<uint32_t *>(ops)[i] = reinterpret_cast<const uint32_t *>(gops)[i];
-    if (tid < 16) hpos[tid] = g.hpos[tid];
-    for (uint32_t r = tid; r < rows; r += blockDim.x) {
-        uint64_t o = 0;
-        for (uint32_t j = 0; j < g.H; j++) o |= (uint64_t)((r >> j) & 1) << g.hpos[j];
-        row_off[r] = o;
-    }
-    if (tid == 0) {
-        s_fail = 0;
-        mbar_init(&bar, 1);
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    }
-    __syncthreads();
-    bool has_arith = false;
-    for (int o = 0; o < nops; o++) has_arith |= ops[o].kind == MOP_U1 || ops[o].kind == MOP_D1 || ops[o].kind == MOP_DK;
-    if (tid < nops) {
-        const MicroOp &op = ops[tid];
-        if (op.kind == MOP_U1 || op.kind == MOP_D1) {
-            const int cnt = op.kind == MOP_U1 ? 8 : 4;
-            for (int i = 0; i < cnt; i++) {
-                if constexpr (A == AR_DF)
-                    coef[tid].v[i] = df_from_f64(op.m[i]);
-                else
-                    coef[tid].v[i] = (T)op.m[i];
-            }
-        }
-    }
-    __syncthreads();
+    T *sim = sre + (1u << (g.L + g.H));
+    sweep_init(c);
+    load_job(c, gops, nops, g.L, g.H, g.hpos);
     uint32_t phase = 0;
-    for (uint64_t t = blockIdx.x; t < g.ntiles; t += gridDim.x) {
-        const uint64_t base = tile_base(t, g.L, hpos, g.H);
-        if (warp == 0) {
-            if (lane == 0) mbar_expect_tx(&bar, 2u * rows * row_bytes);
-            __syncwarp();
-            for (uint32_t r = lane; r < rows; r += 32) {
-                const uint64_t gi = base | row_off[r];
-                bulk_load(sre + (size_t)r * row_elems, re + gi, row_bytes, &bar);
-                bulk_load(sim + (size_t)r * row_elems, im + gi, row_bytes, &bar);
-            }
+    for (uint64_t t = blockIdx.x; t < g.ntiles; t += gridDim.x)
+        if (!process_tile(c, re, im, t, tables, sre, sim, phase)) break;
+    sweep_exit(c, phase, err);
+}
+
+// Many states in one launch (the serving engine's packed step): the tiles
+// of all jobs form one index space; a CTA switches job when its next tile
+// belongs to another state.
+template <typename T, int A>
+__global__ void __launch_bounds__(kSweepThreads, kSweepCtasPerSm)
+    k_sweep_multi(const char *__restrict__ blob, int *__restrict__ err) {
+    extern __shared__ __align__(1024) unsigned char smem[];
+    __shared__ SweepSmem<T, A> c;
+    const SweepBatch *hdr = reinterpret_cast<const SweepBatch *>(blob);
+    const SweepJob *jobs = reinterpret_cast<const SweepJob *>(blob + sizeof(SweepBatch));
+    const uint32_t njobs = hdr->njobs;
+    const uint64_t total = hdr->total_tiles;
+    sweep_init(c);
+    uint32_t phase = 0;
+    int cur = -1;
+    for (uint64_t t = blockIdx.x; t < total; t += gridDim.x) {
+        uint32_t lo = 0, hi = njobs;  // last job with tile_start <= t
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) / 2;
+            if (jobs[mid].tile_start <= t) lo = mid;
+            else hi = mid;
         }
-        // Every thread waits; a timeout anywhere makes all threads leave together.
-        if (!mbar_wait(&bar, phase)) s_fail = 1;
-        __syncthreads();
-        if (s_fail) break;
-        phase ^= 1;
-        if constexpr (A == AR_DF) {
-            double *dr = reinterpret_cast<double *>(sre), *di = reinterpret_cast<double *>(sim);
-            float2 *fr = reinterpret_cast<float2 *>(sre), *fi = reinterpret_cast<float2 *>(sim);
-            if (has_arith) {
-                for (uint32_t v = tid; v < size; v += blockDim.x) {
-                    fr[v] = df_from_f64(dr[v]);
-                    fi[v] = df_from_f64(di[v]);
-                }
-                __syncthreads();
-            }
-            apply_ops<T, A, float2>(fr, fi, ops, coef, nops, base, size, tables);
-            if (has_arith) {
-                for (uint32_t v = tid; v < size; v += blockDim.x) {
-                    dr[v] = df_to_f64(fr[v]);
-                    di[v] = df_to_f64(fi[v]);
-                }
-            }
-        } else {
-            apply_ops<T, A, T>(sre, sim, ops, coef, nops, base, size, tables);
+        const SweepJob &J = jobs[lo];
+        if ((int)lo != cur) {
+            load_job(c, reinterpret_cast<const MicroOp *>(blob + J.ops_off), (int)J.nops, J.L, J.H, J.hpos);
+            cur = (int)lo;
         }
-        fence_async_smem();
-        __syncthreads();
-        if (warp == 0) {
-            for (uint32_t r = lane; r < rows; r += 32) {
-                const uint64_t gi = base | row_off[r];
-                bulk_store(re + gi, sre + (size_t)r * row_elems, row_bytes);
-                bulk_store(im + gi, sim + (size_t)r * row_elems, row_bytes);
-            }
-            bulk_commit();
-            bulk_wait_read_all();  // the buffer is free once the stores have read it
-        }
-        __syncthreads();
+        T *sre = reinterpret_cast<T *>(smem);
+        T *sim = sre + (1u << (J.L + J.H));
+        if (!process_tile(c, reinterpret_cast<T *>(J.re), reinterpret_cast<T *>(J.im), t - J.tile_start,
+                          blob + J.tables_off, sre, sim, phase))
+            break;
     }
-    if (s_fail && tid == 0) {
-        // Give the loads still in flight a bounded chance to land before exit.
-        mbar_wait(&bar, phase);
-        atomicExch(err, 1);
-    }
-    if (warp == 0) bulk_wait_all();
+    sweep_exit(c, phase, err);
 }
 
 template <typename T, int A>
@@ -325,7 +407,28 @@ int run_sweep(zc_state *st, const SweepGeom &g, const MicroOp *dev_ops, int nops
     return ZC_OK;
 }
 
+template <typename T, int A>
+int run_sweep_multi(cudaStream_t stream, int num_sms, const char *dev_blob, int *d_err) {
+    static bool attr = false;
+    if (!attr) {
+        ZC_CUDA(cudaFuncSetAttribute(k_sweep_multi<T, A>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kSweepSmemBytes));
+        attr = true;
+    }
+    k_sweep_multi<T, A><<<num_sms * kSweepCtasPerSm, kSweepThreads, kSweepSmemBytes, stream>>>(dev_blob, d_err);
+    ZC_CUDA(cudaGetLastError());
+    return ZC_OK;
+}
+
 }  // namespace
+
+int launch_sweep_multi(cudaStream_t stream, int num_sms, int prec, bool exact, const char *dev_blob, int *d_err) {
+    if (prec == 64)
+        return exact ? run_sweep_multi<double, AR_EXACT>(stream, num_sms, dev_blob, d_err)
+                     : run_sweep_multi<double, AR_DF>(stream, num_sms, dev_blob, d_err);
+    return exact ? run_sweep_multi<float, AR_EXACT>(stream, num_sms, dev_blob, d_err)
+                 : run_sweep_multi<float, AR_FMA>(stream, num_sms, dev_blob, d_err);
+}
 
 int launch_sweep(zc_state *st, const SweepGeom &g, const MicroOp *dev_ops, int nops, const char *dev_tables,
                  bool exact) {

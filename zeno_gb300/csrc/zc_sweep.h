@@ -31,4 +31,21 @@ struct MicroOp {
     double m[8];
 };
 
+// Packed launch over many states: header, then jobs, then each job's
+// micro-ops and tables at the given byte offsets of the same blob.
+struct SweepBatch {
+    uint32_t njobs, pad;
+    uint64_t total_tiles;
+};
+
+struct SweepJob {
+    void *re, *im;  // the state's device arrays
+    uint32_t L, H, nops, pad;
+    uint32_t hpos[8];
+    uint64_t ntiles;
+    uint64_t tile_start;  // first tile of this job in the packed index space
+    uint64_t ops_off;     // byte offset of its MicroOps in the blob (16-byte aligned)
+    uint64_t tables_off;  // byte offset of its tables in the blob
+};
+
 }  // namespace zc

@@ -76,6 +76,19 @@ int zc_norm_sqr(zc_state *st, double *out);
 /* Backend::finish: wait for all queued GPU work. */
 int zc_finish(zc_state *st);
 
+/* Backend::sample without any allocation (no counterpart in the reference).
+ * For callers that cannot let the library allocate device memory when they
+ * sample: runtimes that carve all device memory into their own pool at
+ * start-up, loops that must not stall on cudaMalloc/cudaFree, or code that
+ * is recording a stream capture. Same indices as zc_sample. Its scratch is
+ * a fixed ~0.9 MiB device array that every GPU loading the library keeps
+ * until exit. Limits: <= 30 qubits, <= 16384 shots; larger requests get
+ * ZC_ERR_INVALID. Queued ops must be flushed first (zc_finish). The first
+ * call on a device resolves the array's device address, so make that call
+ * before any stream capture. All calls share the array: calls that overlap
+ * (on the GPU or from several threads) race. */
+int zc_sample_noalloc(zc_state *st, uint64_t shots, uint64_t seed, uint64_t *out);
+
 /* Thread-local text of the last error. */
 const char *zc_last_error(void);
 

@@ -32,7 +32,7 @@ EXPORTS = (
     "zc_statevector", "zc_norm_sqr", "zc_finish", "zc_last_error", "zc_device_budget", "zc_state_bytes",
     "zc_max_qubits", "zc_load_state", "zc_get_stream", "zc_get_counters", "zc_compile", "zc_program_free",
     "zc_program_get_info", "zc_program_get_op", "zc_program_get_final", "zc_run", "zc_profile",
-    "zc_profile_read",
+    "zc_profile_read", "zc_sample_noalloc",
 )
 
 
@@ -159,6 +159,7 @@ def load() -> C.CDLL:
         "zc_program_get_final": ([vp, C.c_size_t, P(u32), P(u32)], i32),
         "zc_run": ([vp, P(RunOptions), P(RunResultC), P(u64), P(u64), C.c_size_t, P(dbl)], i32),
         "zc_profile": ([vp, i32], i32),
+        "zc_sample_noalloc": ([vp, u64, u64, P(u64)], i32),
         "zc_profile_read": ([vp, P(KernelStat), i32, P(i32)], i32),
     }
     for name, (args, res) in sig.items():
@@ -228,6 +229,13 @@ class CudaBackend:
     def sample(self, shots: int, seed: int) -> np.ndarray:
         out = np.zeros(max(1, shots), dtype=np.uint64)
         _check(load().zc_sample(self._h, shots, seed, out.ctypes.data_as(C.POINTER(C.c_uint64))))
+        return out[:shots]
+
+    def sample_noalloc(self, shots: int, seed: int) -> np.ndarray:
+        """`sample` through the entry point that allocates nothing (for callers
+        that cannot allocate device memory at sampling time); flush first."""
+        out = np.zeros(max(1, shots), dtype=np.uint64)
+        _check(load().zc_sample_noalloc(self._h, shots, seed, out.ctypes.data_as(C.POINTER(C.c_uint64))))
         return out[:shots]
 
     def statevector(self) -> np.ndarray:

@@ -115,6 +115,23 @@ def batched_trajectories(zc, C):
             "speedup_vs_plain": (4096 / tb) * tp}
 
 
+def serving_sample(zc):
+    """A short request stream (8..22 qubits, gate-mix circuits, Poisson
+    arrivals at 3000 req/s): the continuous-batching server against one
+    circuit per call in arrival order."""
+    from zeno_gb300 import serve
+
+    reqs = serve.request_stream(300, rate=3000.0, master_seed=2024, n_max=22)
+    serve.compile_requests(reqs)
+    s = serve.serve_stream(reqs)
+    plain = serve.request_stream(300, rate=3000.0, master_seed=2024, n_max=22)
+    for a, b in zip(plain, reqs):
+        a.program = b.program
+    pl = serve.plain_stream(plain)
+    return {"workload": "300 requests, 8..22 qubits, depth U[4,60], shots 1..8192, Poisson 3000 req/s, 5% f64",
+            "server": s, "one_per_call": pl, "throughput_ratio": s["circuits_per_s"] / pl["circuits_per_s"]}
+
+
 class Clocks:
     """nvidia-smi clock / throttle sampling during the timed region."""
 
@@ -359,6 +376,7 @@ def main():
                        "path": "zc_run: allocate state, per-op host->device tables, kernels, sample, read indices"}
     if rank == 0 and not a.no_extras:
         line["batched_trajectories"] = batched_trajectories(zc, C)
+        line["serving"] = serving_sample(zc)
     if rank == 0 and a.mode == "fast" and not a.no_check:
         line["accuracy"] = accuracy_check(a, zc, C)
     if rank == 0 and not a.no_cpu:

@@ -1,0 +1,122 @@
+"""Measurement suite for the workloads beside the headline benchmark.
+
+  python -m zeno_gb300.suite qft        # QFT 24/28 qubits, f64/f32, exact/fast, 8192 shots
+  python -m zeno_gb300.suite fusion     # 30q depth-40 f64 at fusion widths K = 1..5
+  python -m zeno_gb300.suite big        # 33q depth-40 f64 (128 GiB state)
+  python -m zeno_gb300.suite serving    # request stream at several arrival rates, server vs one-per-call
+  python -m zeno_gb300.suite trajectories  # 4096 noisy 16q trajectories, batched vs per-shot
+
+Each prints JSON lines. Times are wall-clock around complete runs
+(`zc_run`: state allocation, ops, sampling), the semantics of zeno's
+sim_time (src/exec.rs:372-381).
+"""
+
+import argparse
+import json
+import math
+import os
+import sys
+import time
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+from zeno_gb300 import backend as zb  # noqa: E402
+from zeno_gb300 import circuit as C  # noqa: E402
+
+
+def _run(p, prog, prec, flags, shots, seed):
+    t0 = time.perf_counter()
+    r = zb.run(p, shots=shots, seed=seed, precision=prec, flags=flags, program=prog)
+    return time.perf_counter() - t0, r
+
+
+def qft(args):
+    for n in (24, 28):
+        c, x = C.qft_circuit(n, 11)
+        p = c.to_program()
+        prog = zb.compile(p, 1)
+        for prec in (64, 32):
+            for flags, mode in ((zb.FLAG_EXACT, "exact"), (zb.FLAG_FAST, "fast")):
+                _run(p, prog, prec, flags, 8192, 3)
+                t, r = _run(p, prog, prec, flags, 8192, 3)
+                print(json.dumps({"workload": "qft", "qubits": n, "precision": prec, "mode": mode, "seconds": t,
+                                  "sweeps": r.sweeps, "launches": r.launches, "ops": len(prog.ops),
+                                  "input_gates": r.stats["input_gates"],
+                                  "amp_updates_per_s": r.stats["input_gates"] * 2.0 ** n / t}), flush=True)
+
+
+def fusion(args):
+    n = args.qubits
+    p = C.matching_circuit(n, 40, 7).to_program()
+    for k in range(1, 6):
+        prog = zb.compile(p, k)
+        for flags, mode in ((zb.FLAG_FAST, "fast"),):
+            t, r = _run(p, prog, 64, flags, 1024, 7)
+            S = 2.0 ** n * 16
+            print(json.dumps({"workload": "%dq d40 f64" % n, "fusion": k, "mode": mode, "seconds": t,
+                              "ops": len(prog.ops), "max_fused": prog.stats["max_fused"], "sweeps": r.sweeps,
+                              "launches": r.launches, "sweep_GBps": r.bytes_moved / t / 1e9,
+                              "state_GiB": S / 2**30}), flush=True)
+
+
+def big(args):
+    n = args.qubits
+    p = C.matching_circuit(n, 40, 7).to_program()
+    prog = zb.compile(p, 1)
+    t, r = _run(p, prog, 64, zb.FLAG_FAST, 1024, 7)
+    print(json.dumps({"workload": "%dq d40 f64 fast" % n, "seconds": t, "sweeps": r.sweeps,
+                      "launches": r.launches, "state_GiB": 2.0 ** n * 16 / 2**30,
+                      "hbm_GBps_of_passes": r.bytes_moved / t / 1e9}), flush=True)
+
+
+def serving(args):
+    from zeno_gb300 import serve
+
+    for rate in args.rates:
+        reqs = serve.request_stream(args.requests, rate=rate, master_seed=2024, n_max=args.n_max)
+        serve.compile_requests(reqs)
+        s = serve.serve_stream(reqs)
+        reqs2 = serve.request_stream(args.requests, rate=rate, master_seed=2024, n_max=args.n_max)
+        for a, b in zip(reqs2, reqs):
+            b_prog = b.program
+            a.program = b_prog
+        pl = serve.plain_stream(reqs2)
+        print(json.dumps({"workload": "serving", "rate_per_s": rate, "requests": args.requests,
+                          "qubits": [8, args.n_max], "server": s, "plain": pl,
+                          "throughput_ratio": s["circuits_per_s"] / pl["circuits_per_s"]}), flush=True)
+
+
+def trajectories(args):
+    noise = zb.NoiseModel(depolarizing_1q=1e-3, depolarizing_2q=1e-2, amplitude_damping=1e-3,
+                          readout_flip_0to1=0.02, readout_flip_1to0=0.02)
+    p = C.matching_circuit(16, 20, 7).to_program()
+    prog = zb.compile(p, 0)
+    zb.run(p, shots=256, seed=1, precision=32, noise=noise, program=prog)
+    t0 = time.perf_counter()
+    r = zb.run(p, shots=4096, seed=2, precision=32, noise=noise, program=prog)
+    tb = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    zb.run(p, shots=32, seed=2, precision=32, noise=noise, program=prog, flags=zb.FLAG_PER_SHOT)
+    tp = (time.perf_counter() - t0) / 32
+    print(json.dumps({"workload": "16q d20 noisy, 4096 trajectories", "batched_seconds": tb,
+                      "trajectories_per_s": 4096 / tb, "per_shot_trajectories_per_s": 1 / tp,
+                      "launches": r.launches, "keys": len(r.counts)}), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("what", choices=["qft", "fusion", "big", "serving", "trajectories"])
+    ap.add_argument("--qubits", type=int, default=None)
+    ap.add_argument("--requests", type=int, default=1000)
+    ap.add_argument("--rates", type=float, nargs="*", default=[100.0, 1000.0, 10000.0])
+    ap.add_argument("--n-max", type=int, default=26)
+    a = ap.parse_args()
+    if a.qubits is None:
+        a.qubits = {"fusion": 30, "big": 33}.get(a.what, 30)
+    zb.load()
+    globals()[a.what](a)
+
+
+if __name__ == "__main__":
+    main()

@@ -35,6 +35,7 @@ extern "C" {
 #define ZC_FLAG_NO_SWEEPS 2u  /* one launch per op: disables multi-op sweep scheduling */
 #define ZC_FLAG_FORCE_SWEEPS 4u /* schedule sweeps even for small states (testing) */
 #define ZC_FLAG_PER_SHOT 8u   /* noisy runs: replay shot by shot (zeno's order and RNG) instead of batching */
+#define ZC_FLAG_TENSOR 16u    /* f32 states: dense k>=3 blocks as 3xTF32 tensor-core GEMMs (FP32 accumulation) */
 
 typedef struct zc_state zc_state;
 

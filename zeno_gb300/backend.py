@@ -22,7 +22,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_lib", "libzeno_cuda.so")
 
 ZC_OK, ZC_ERR_INVALID, ZC_ERR_MEMORY, ZC_ERR_CUDA, ZC_ERR_UNSUPPORTED = 0, 1, 2, 3, 4
-FLAG_EXACT, FLAG_FAST, FLAG_NO_SWEEPS, FLAG_FORCE_SWEEPS, FLAG_PER_SHOT = 0, 1, 2, 4, 8
+FLAG_EXACT, FLAG_FAST, FLAG_NO_SWEEPS, FLAG_FORCE_SWEEPS, FLAG_PER_SHOT, FLAG_TENSOR = 0, 1, 2, 4, 8, 16
 OP_UNITARY, OP_DIAG, OP_CX, OP_MEASURE, OP_RESET, OP_SWAP = 0, 1, 2, 3, 4, 6
 
 # Every entry point the header declares; the CPU test suite checks exports.

@@ -142,11 +142,44 @@ static constexpr size_t kQueueWindow = 2048;  // ops examined per sweep plan
 static constexpr size_t kQueueFlushAt = 8192; // queue length that forces a flush
 static constexpr uint32_t kMinSweepQubits = 14;
 
+// Real 2D x 2D form [[Mr, -Mi], [Mi, Mr]] of a complex D x D matrix, split
+// into TF32 parts (round to nearest, ties away: the rounding of cvt.rna.tf32).
+static float tf32_rna(float x) {
+    uint32_t u;
+    memcpy(&u, &x, 4);
+    if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x1000u) & 0xffffe000u;
+    float r;
+    memcpy(&r, &u, 4);
+    return r;
+}
+
+static int stage_tc_matrix(zc_state *st, const double *mat, uint32_t k, const void **dev) {
+    const size_t D = (size_t)1 << k, R = 2 * D;
+    std::vector<float> a(2 * R * R);
+    float *ah = a.data(), *al = a.data() + R * R;
+    for (size_t r = 0; r < R; r++)
+        for (size_t c = 0; c < R; c++) {
+            const size_t i = r % D, j = c % D;
+            const double mr = mat[2 * (i * D + j)], mi = mat[2 * (i * D + j) + 1];
+            const double v = (r < D) == (c < D) ? mr : (r < D ? -mi : mi);
+            const float h = tf32_rna((float)v);
+            ah[r * R + c] = h;
+            al[r * R + c] = tf32_rna((float)(v - (double)h));
+        }
+    return arena_put(st, a.data(), a.size() * sizeof(float), dev);
+}
+
 int launch_single(zc_state *st, const QOp &op) {
     const bool ex = exact(st);
     switch (op.kind) {
         case Q_UNITARY: {
             if (op.k == 1) return launch_1q(st, op.qs[0], op.data.data(), ex);
+            if (op.k >= 3 && st->prec == 32 && (st->flags & ZC_FLAG_TENSOR)) {
+                const void *dev = nullptr;
+                int rc = stage_tc_matrix(st, op.data.data(), op.k, &dev);
+                if (rc) return rc;
+                return launch_block_tc(st, op.qs, op.k, (const float *)dev);
+            }
             const void *dev = nullptr;
             int rc = stage_table(st, op.data.data(), (size_t)1 << (2 * op.k), &dev);
             if (rc) return rc;
@@ -372,12 +405,18 @@ static int enqueue(zc_state *st, QOp &&op) {
 }
 
 static int check_device_error(zc_state *st) {
-    int h = 0;
-    ZC_CUDA(cudaMemcpyAsync(&h, st->d_err, sizeof(int), cudaMemcpyDeviceToHost, st->stream));
+    int h[kErrWords] = {};
+    ZC_CUDA(cudaMemcpyAsync(h, st->d_err, sizeof(h), cudaMemcpyDeviceToHost, st->stream));
     ZC_CUDA(cudaStreamSynchronize(st->stream));
-    if (h) {
-        cudaMemsetAsync(st->d_err, 0, sizeof(int), st->stream);
-        return fail(ZC_ERR_CUDA, "sweep kernel gave up waiting for a bulk copy (device wait limit reached)");
+    if (h[0]) {
+        cudaMemsetAsync(st->d_err, 0, sizeof(h), st->stream);
+        char buf[320];
+        snprintf(buf, sizeof(buf),
+                 "sweep kernel %s (cta %d tile %d phase %d barrier %08x%08x L %d H %d ops %d tiles done %d index %08x)",
+                 h[0] == 1 ? "gave up waiting for a bulk copy (device wait limit reached)"
+                           : "found a tile index out of range",
+                 h[1], h[2], h[3], (unsigned)h[5], (unsigned)h[4], h[6], h[7], h[8], h[9], (unsigned)h[10]);
+        return fail(ZC_ERR_CUDA, buf);
     }
     return ZC_OK;
 }
@@ -474,8 +513,8 @@ int zc_create_ex(uint32_t n, int prec, uint32_t flags, zc_state **out) {
     TRY(cudaMalloc(&st->arena.dev, kArenaBytes));
     st->arena.cap = kArenaBytes;
     TRY(cudaMalloc(&st->d_scalar, sizeof(double)));
-    TRY(cudaMalloc(&st->d_err, sizeof(int)));
-    TRY(cudaMemsetAsync(st->d_err, 0, sizeof(int), st->stream));
+    TRY(cudaMalloc(&st->d_err, kErrWords * sizeof(int)));
+    TRY(cudaMemsetAsync(st->d_err, 0, kErrWords * sizeof(int), st->stream));
     TRY(cudaMallocHost(&st->h_scalar, sizeof(double)));
 #undef TRY
     rc = launch_reset(st);
@@ -546,9 +585,9 @@ int zc_prob_one(zc_state *st, uint32_t q, double *out) {
     int rc = flush(st);
     if (rc) return rc;
     size_t nch = 0;
-    rc = launch_chunk_sums(st, 1, q, &nch);
+    rc = launch_chunk_sums(st, 1, q, &nch, exact(st));
     if (rc) return rc;
-    rc = launch_serial_sum(st, nch);
+    rc = launch_serial_sum(st, nch, exact(st));
     if (rc) return rc;
     return sync_read_scalar(st, out);
 }
@@ -577,9 +616,9 @@ int zc_norm_sqr(zc_state *st, double *out) {
     int rc = flush(st);
     if (rc) return rc;
     size_t nch = 0;
-    rc = launch_chunk_sums(st, 0, 0, &nch);
+    rc = launch_chunk_sums(st, 0, 0, &nch, exact(st));
     if (rc) return rc;
-    rc = launch_serial_sum(st, nch);
+    rc = launch_serial_sum(st, nch, exact(st));
     if (rc) return rc;
     return sync_read_scalar(st, out);
 }
@@ -594,7 +633,7 @@ int zc_sample(zc_state *st, uint64_t shots, uint64_t seed, uint64_t *out) {
     int rc = flush(st);
     if (rc) return rc;
     size_t nch = 0;
-    rc = launch_chunk_sums(st, 0, 0, &nch);
+    rc = launch_chunk_sums(st, 0, 0, &nch, exact(st));
     if (rc) return rc;
     std::vector<double> sums(nch);
     ZC_CUDA(cudaMemcpyAsync(sums.data(), st->d_part, nch * sizeof(double), cudaMemcpyDeviceToHost, st->stream));
@@ -616,18 +655,20 @@ int zc_sample(zc_state *st, uint64_t shots, uint64_t seed, uint64_t *out) {
     }
     const uint64_t chunk_len = st->len < (1ull << kSampleChunkLog2) ? st->len : (1ull << kSampleChunkLog2);
     const size_t us_b = shots * sizeof(double), out_b = shots * sizeof(uint64_t);
-    const size_t cs_b = touched.size() * sizeof(SampleChunk);
-    rc = grow(&st->d_samp, &st->samp_cap, us_b + out_b + cs_b + 64);
+    const size_t cs_b = (touched.size() * sizeof(SampleChunk) + 255) & ~(size_t)255;
+    const size_t sc_b = sample_scan_scratch(touched.size(), chunk_len, exact(st));
+    rc = grow(&st->d_samp, &st->samp_cap, us_b + out_b + cs_b + sc_b + 64);
     if (rc) return rc;
     char *base = (char *)st->d_samp;
     double *d_us = (double *)base;
     uint64_t *d_out = (uint64_t *)(base + us_b);
     SampleChunk *d_cs = (SampleChunk *)(base + us_b + out_b);
+    void *d_scratch = base + us_b + out_b + cs_b;
     ZC_CUDA(cudaMemcpyAsync(d_us, us.data(), us_b, cudaMemcpyHostToDevice, st->stream));
     ZC_CUDA(cudaMemsetAsync(d_out, 0, out_b, st->stream));
     if (!touched.empty())
         ZC_CUDA(cudaMemcpyAsync(d_cs, touched.data(), cs_b, cudaMemcpyHostToDevice, st->stream));
-    rc = launch_sample_scan(st, d_cs, touched.size(), d_us, d_out, chunk_len);
+    rc = launch_sample_scan(st, d_cs, touched.size(), d_us, d_out, chunk_len, exact(st), d_scratch);
     if (rc) return rc;
     ZC_CUDA(cudaMemcpyAsync(out, d_out, out_b, cudaMemcpyDeviceToHost, st->stream));
     ZC_CUDA(cudaStreamSynchronize(st->stream));

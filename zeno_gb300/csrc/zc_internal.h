@@ -24,6 +24,7 @@ int cuda_fail(cudaError_t e, const char *where);
 constexpr int kMaxUnitaryQubits = 7;
 constexpr int kMaxDiagQubits = 12;
 constexpr int kSampleChunkLog2 = 16;  // sample.rs CHUNK = 1 << 16
+constexpr int kErrWords = 16;         // device error record (d_err) in ints
 
 // Device parameter arena: tables (matrices, diagonals) for queued ops are
 // staged in pinned host memory and copied into a device ring. Wrapping the
@@ -106,19 +107,22 @@ struct ProfScope {
 
 int launch_1q(zc_state *st, uint32_t q, const double *m8, bool exact);
 int launch_kq(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat, bool exact);
+// Dense k-qubit block (k = 3..7) on tensor cores, f32 state, 3xTF32 (zc_tc.cu).
+int launch_block_tc(zc_state *st, const uint32_t *qs, uint32_t k, const float *dev_a);
 int launch_diag1(zc_state *st, uint32_t q, const double *d4, bool exact);
 int launch_diagk(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_diag, bool exact);
 int launch_cx(zc_state *st, uint32_t c, uint32_t t);
 int launch_swap(zc_state *st, uint32_t a, uint32_t b);
 int launch_reset(zc_state *st);
 int launch_collapse(zc_state *st, uint32_t q, int outcome, double scale64);
-// f64 partial sums of |amp|^2 over chunks of 2^16 (serial within a chunk).
+// f64 partial sums of |amp|^2 over chunks of 2^16 (exact: serial within a
+// chunk in the reference's order; otherwise parallel double-float).
 // mode 0: all amplitudes (norm / sampler pass 1); mode 1: the q=1 half of
 // qubit q (prob_one). Writes nchunks partials to st->d_part.
-int launch_chunk_sums(zc_state *st, int mode, uint32_t q, size_t *nchunks);
-// Serial in-order sum of st->d_part[0..nchunks) into st->d_scalar.
-int launch_serial_sum(zc_state *st, size_t nchunks);
-// Sampler pass 2 (sample.rs:64-108): one thread per touched chunk.
+int launch_chunk_sums(zc_state *st, int mode, uint32_t q, size_t *nchunks, bool exact);
+// Sum of st->d_part[0..nchunks) into st->d_scalar (exact: serial, in order).
+int launch_serial_sum(zc_state *st, size_t nchunks, bool exact);
+// Sampler pass 2 (sample.rs:64-108): a touched chunk and its draws.
 struct SampleChunk {
     uint64_t chunk;  // chunk index
     uint64_t s0, s1; // draw range
@@ -148,7 +152,9 @@ struct TrajNoise;
 int launch_trajectories(zc_state *st, uint32_t n, const TrajOp *d_ops, int nops, const double *d_mats,
                         const uint32_t *d_fq, const uint32_t *d_fc, int nfinal, const TrajNoise &nz, uint64_t ntraj,
                         uint64_t seed, uint64_t *d_out, void *d_work, int ctas);
+// d_scratch: sample_scan_scratch(nchunks, chunk_len, exact) bytes of device memory.
 int launch_sample_scan(zc_state *st, const SampleChunk *d_chunks, size_t nchunks, const double *d_us,
-                       uint64_t *d_out, uint64_t chunk_len);
+                       uint64_t *d_out, uint64_t chunk_len, bool exact, void *d_scratch);
+size_t sample_scan_scratch(size_t nchunks, uint64_t chunk_len, bool exact);
 
 }  // namespace zc

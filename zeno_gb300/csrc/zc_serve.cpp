@@ -295,7 +295,10 @@ int zc_server_create(const zc_server_options *opt, zc_server **out) {
     c->d_part = nullptr;
     if ((e = cudaMalloc(&c->d_part, chunks * sizeof(double))) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc"));
     c->part_cap = chunks;
-    const size_t samp = kServeMaxShots * (sizeof(double) + sizeof(uint64_t) + sizeof(SampleChunk)) + 64;
+    const size_t touched_max = std::min<size_t>(kServeMaxShots, chunks);
+    const size_t samp = kServeMaxShots * (sizeof(double) + sizeof(uint64_t)) +
+                        ((kServeMaxShots * sizeof(SampleChunk) + 255) & ~(size_t)255) +
+                        sample_scan_scratch(touched_max, (size_t)1 << kSampleChunkLog2, (s->flags & ZC_FLAG_FAST) == 0) + 64;
     if ((e = cudaMalloc(&c->d_samp, samp)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc"));
     c->samp_cap = samp;
     for (auto &g : s->groups) {

@@ -24,7 +24,8 @@ namespace {
 
 constexpr int kSweepThreads = 256;
 constexpr int kSweepCtasPerSm = 3;
-constexpr unsigned kSpinLimit = 1u << 26;  // bounded mbarrier waits
+constexpr unsigned kSpinLimit = 1u << 26;  // bounded mbarrier waits: polls
+constexpr uint64_t kWaitNs = 2000000000ull; // and wall time (2 s)
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -39,9 +40,17 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                  : "memory");
 }
 
-// Bounded wait on phase `parity`; returns false if the limit was reached.
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Bounded wait on phase `parity`: gives up after kSpinLimit polls or
+// kWaitNs of wall time, whichever comes first; returns false then.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     const uint32_t a = smem_addr(bar);
+    const uint64_t t0 = global_ns();
     for (unsigned it = 0; it < kSpinLimit; ++it) {
         uint32_t done;
         asm volatile(
@@ -52,6 +61,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
+        if ((it & 63) == 63 && global_ns() - t0 > kWaitNs) break;
     }
     return false;
 }
@@ -147,15 +157,104 @@ __device__ __forceinline__ uint32_t jouter(const MicroOp &op, uint64_t base) {
     return jo;
 }
 
+// Apply G consecutive one-qubit micro-ops (ops[o..o+G), distinct tile bits)
+// to register-held groups of 2^G elements: each gate updates the same pairs
+// with the same arithmetic, in the same order, as one op at a time.
+template <typename T, int A, typename R, int G>
+__device__ void apply_u1_group(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *coef, int o, uint32_t size,
+                               uint32_t *bad) {
+    constexpr int E = 1 << G;
+    uint32_t bits[G], sorted[G];
+#pragma unroll
+    for (int g = 0; g < G; g++) bits[g] = sorted[g] = ops[o + g].a;
+#pragma unroll
+    for (int i = 1; i < G; i++)
+#pragma unroll
+        for (int j = i; j > 0; j--)
+            if (sorted[j] < sorted[j - 1]) {
+                const uint32_t x = sorted[j];
+                sorted[j] = sorted[j - 1];
+                sorted[j - 1] = x;
+            }
+    for (uint32_t p = threadIdx.x; p < size / E; p += blockDim.x) {
+        uint32_t v = p;
+#pragma unroll
+        for (int g = 0; g < G; g++) v = ((v >> sorted[g]) << (sorted[g] + 1)) | (v & ((1u << sorted[g]) - 1));
+        uint32_t idx[E];
+        R xr[E], xi[E];
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            uint32_t w = v;
+#pragma unroll
+            for (int g = 0; g < G; g++)
+                if ((e >> g) & 1) w |= 1u << bits[g];
+            if (w >= size) {  // cannot happen for tile bits < log2(size); recorded, access skipped
+                *bad = w | 0x80000000u;
+                w = 0;
+            }
+            idx[e] = w;
+            xr[e] = sr[w];
+            xi[e] = si[w];
+        }
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            if constexpr (A == AR_DF) {
+                MatDF m;
+#pragma unroll
+                for (int i = 0; i < 8; i++) m.v[i] = coef[o + g].v[i];
+#pragma unroll
+                for (int e = 0; e < E; e++)
+                    if (!((e >> g) & 1)) pair_update_df(m, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+            } else {
+                Mat2<T> m;
+#pragma unroll
+                for (int i = 0; i < 8; i++) m.v[i] = coef[o + g].v[i];
+#pragma unroll
+                for (int e = 0; e < E; e++)
+                    if (!((e >> g) & 1))
+                        pair_update<T, A == AR_EXACT>(m, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+            }
+        }
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            sr[idx[e]] = xr[e];
+            si[idx[e]] = xi[e];
+        }
+    }
+}
+
 // Apply the sweep's micro-ops to one tile. For A == AR_DF the tile's f64
 // slots hold (hi, lo) float pairs (R = float2); otherwise R = T.
 template <typename T, int A, typename R>
 __device__ void apply_ops(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *coef, int nops, uint64_t base,
-                          uint32_t size, const char *tables) {
+                          uint32_t size, const char *tables, uint32_t *bad) {
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int o = 0; o < nops; o++) {
         const MicroOp &op = ops[o];
         if (op.kind == MOP_U1) {
+            // runs of up to three one-qubit ops on distinct bits share one
+            // register pass (two for f64 states outside FMA mode, which would
+            // spill at the 80-register cap with three)
+            constexpr int kMaxGroup = sizeof(T) == 8 && A != AR_FMA ? 2 : 3;
+            int g = 1;
+            while (g < kMaxGroup && o + g < nops && ops[o + g].kind == MOP_U1) {
+                bool distinct = true;
+                for (int h = 0; h < g; h++) distinct &= ops[o + h].a != ops[o + g].a;
+                if (!distinct) break;
+                g++;
+            }
+            if (kMaxGroup == 3 && g == 3) {
+                apply_u1_group<T, A, R, kMaxGroup>(sr, si, ops, coef, o, size, bad);
+                o += 2;
+                __syncthreads();
+                continue;
+            }
+            if (g == 2) {
+                apply_u1_group<T, A, R, 2>(sr, si, ops, coef, o, size, bad);
+                o += 1;
+                __syncthreads();
+                continue;
+            }
             const uint32_t b = op.a;
             if constexpr (A == AR_DF) {
                 MatDF m;
@@ -215,6 +314,7 @@ struct SweepSmem {
     uint32_t L, H;
     int has_arith;
     int fail;
+    uint32_t fail_tile, done_tiles, bad;
 };
 
 // All threads: make (gops, nops, L, H, hpos) the CTA's current job.
@@ -276,7 +376,10 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
         }
     }
     // Every thread waits; a timeout anywhere makes all threads leave together.
-    if (!mbar_wait(&c.bar, phase)) c.fail = 1;
+    if (!mbar_wait(&c.bar, phase)) {
+        c.fail = 1;
+        c.fail_tile = (uint32_t)t;
+    }
     __syncthreads();
     if (c.fail) return false;
     phase ^= 1;
@@ -290,7 +393,7 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
             }
             __syncthreads();
         }
-        apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables);
+        apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables, &c.bad);
         if (c.has_arith) {
             for (uint32_t v = tid; v < size; v += blockDim.x) {
                 dr[v] = df_to_f64(fr[v]);
@@ -298,7 +401,7 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
             }
         }
     } else {
-        apply_ops<T, A, T>(sre, sim, c.ops, c.coef, c.nops, base, size, tables);
+        apply_ops<T, A, T>(sre, sim, c.ops, c.coef, c.nops, base, size, tables, &c.bad);
     }
     fence_async_smem();
     __syncthreads();
@@ -311,6 +414,7 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
         bulk_commit();
         bulk_wait_read_all();  // the buffer is free once the stores have read it
     }
+    if (tid == 0) c.done_tiles++;
     __syncthreads();
     return true;
 }
@@ -319,18 +423,36 @@ template <typename T, int A>
 __device__ void sweep_init(SweepSmem<T, A> &c) {
     if (threadIdx.x == 0) {
         c.fail = 0;
+        c.fail_tile = c.done_tiles = c.bad = 0;
         mbar_init(&c.bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
 }
 
+// Error record (the first failing CTA fills it): err[0] = 1 wait ran out /
+// 2 index check; then CTA, tile, phase, raw barrier word, L, H, ops, tiles
+// done, offending index.
 template <typename T, int A>
 __device__ void sweep_exit(SweepSmem<T, A> &c, uint32_t phase, int *err) {
-    if (c.fail && threadIdx.x == 0) {
+    if (threadIdx.x == 0 && (c.fail || c.bad)) {
         // Give the loads still in flight a bounded chance to land before exit.
-        mbar_wait(&c.bar, phase);
-        atomicExch(err, 1);
+        if (c.fail) mbar_wait(&c.bar, phase);
+        uint64_t raw;
+        asm volatile("ld.shared.b64 %0, [%1];" : "=l"(raw) : "r"(smem_addr(&c.bar)) : "memory");
+        if (atomicCAS(err, 0, c.fail ? 1 : 2) == 0) {
+            err[1] = (int)blockIdx.x;
+            err[2] = (int)c.fail_tile;
+            err[3] = (int)phase;
+            err[4] = (int)(uint32_t)raw;
+            err[5] = (int)(uint32_t)(raw >> 32);
+            err[6] = (int)c.L;
+            err[7] = (int)c.H;
+            err[8] = c.nops;
+            err[9] = (int)c.done_tiles;
+            err[10] = (int)c.bad;
+            __threadfence();
+        }
     }
     if (threadIdx.x / 32 == 0) bulk_wait_all();
 }

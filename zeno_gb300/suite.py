@@ -104,16 +104,46 @@ def trajectories(args):
                       "launches": r.launches, "keys": len(r.counts)}), flush=True)
 
 
+def tc(args):
+    """28q depth-60 gate mix fused to 5/6/7-qubit blocks on tensor cores (f32,
+    3xTF32) against the FP64 plain run on the GPU (exact mode = oracle bits)."""
+    import numpy as np
+
+    n = args.qubits
+    p = C.mixed_circuit(n, 60, 7).to_program()
+    ref_prog = zb.compile(p, 1)
+    ref = zb.run(p, shots=0, seed=1, precision=64, flags=zb.FLAG_FAST, statevector=True, program=ref_prog)
+    for k in (5, 6, 7):
+        prog = zb.compile(p, k)
+        zb.run(p, shots=0, seed=1, precision=32, flags=zb.FLAG_TENSOR | zb.FLAG_FAST, program=prog)
+        t0 = time.perf_counter()
+        r = zb.run(p, shots=0, seed=1, precision=32, flags=zb.FLAG_TENSOR | zb.FLAG_FAST, statevector=True,
+                   program=prog)
+        t = time.perf_counter() - t0
+        d = float(np.abs(r.statevector - ref.statevector).max())
+        tvd = float(0.5 * np.abs(np.abs(r.statevector) ** 2 - np.abs(ref.statevector) ** 2).sum())
+        print(json.dumps({"workload": "%dq d60 gate mix, fused k=%d, f32 3xTF32" % (n, k), "seconds_incl_readback": t,
+                          "blocks": len(prog.ops), "max_fused": prog.stats["max_fused"],
+                          "max_abs_damp_vs_f64": d, "tvd_vs_f64": tvd}), flush=True)
+    prog1 = zb.compile(p, 1)
+    t0 = time.perf_counter()
+    r = zb.run(p, shots=0, seed=1, precision=32, flags=zb.FLAG_FAST, statevector=True, program=prog1)
+    t = time.perf_counter() - t0
+    d = float(np.abs(r.statevector - ref.statevector).max())
+    print(json.dumps({"workload": "%dq d60 gate mix, unfused sweeps f32 FMA" % n, "seconds_incl_readback": t,
+                      "ops": len(prog1.ops), "max_abs_damp_vs_f64": d}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["qft", "fusion", "big", "serving", "trajectories"])
+    ap.add_argument("what", choices=["qft", "fusion", "big", "serving", "trajectories", "tc"])
     ap.add_argument("--qubits", type=int, default=None)
     ap.add_argument("--requests", type=int, default=1000)
     ap.add_argument("--rates", type=float, nargs="*", default=[100.0, 1000.0, 10000.0])
     ap.add_argument("--n-max", type=int, default=26)
     a = ap.parse_args()
     if a.qubits is None:
-        a.qubits = {"fusion": 30, "big": 33}.get(a.what, 30)
+        a.qubits = {"fusion": 30, "big": 33, "tc": 28}.get(a.what, 30)
     zb.load()
     globals()[a.what](a)
 

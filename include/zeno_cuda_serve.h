@@ -30,6 +30,13 @@ typedef struct {
     uint64_t pending, active, done;
     uint64_t launches, packed_launches, admitted, completed;
     uint64_t pool_used;
+    uint64_t steps;
+    /* cumulative host microseconds: planning + launching the packed steps,
+     * sampling finished requests, waiting for the device at step ends */
+    uint64_t plan_us, sample_us, wait_us;
+    /* cumulative device microseconds between each step's first and last
+     * launch (CUDA events on the server stream) */
+    uint64_t device_us;
 } zc_server_status;
 
 typedef struct zc_server zc_server;

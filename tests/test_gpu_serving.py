@@ -14,10 +14,10 @@ from zeno_gb300 import serve
 pytestmark = pytest.mark.gpu
 
 
-def _requests(ns, seed0):
+def _requests(ns, seed0, depth=None):
     out = []
     for i, n in enumerate(ns):
-        c = C.mixed_circuit(n, 12 + 3 * (i % 5), seed0 + i)
+        c = C.mixed_circuit(n, depth or 12 + 3 * (i % 5), seed0 + i)
         out.append((zb.compile(c.to_program(), 1), n, 500 + 37 * i, 1000 + i))
     return out
 
@@ -82,13 +82,14 @@ def test_admission_by_footprint_and_slots(zc):
 def test_arrivals_while_running_overlap(zc):
     """Requests submitted between steps join the packed launches of requests
     already in flight."""
-    reqs = _requests([18, 18, 9, 9, 9, 9], 7)
+    reqs = _requests([18, 18, 9, 9, 9, 9], 7, depth=120)  # many packed rounds each
     srv = serve.Server(pool_bytes=1 << 30, flags=zb.FLAG_FAST)
     first = [srv.submit(p, 32, s, sd) for p, n, s, sd in reqs[:2]]
-    srv.step()
+    st = srv.step()
+    assert st.active == 2
     late = [srv.submit(p, 32, s, sd) for p, n, s, sd in reqs[2:]]
     st = srv.step()
-    assert st.active >= 3  # the late arrivals are on the device with the first two
+    assert st.active == 6  # the late arrivals are on the device with the first two
     done = set()
     for _ in range(10000):
         st = srv.step()

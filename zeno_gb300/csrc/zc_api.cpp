@@ -421,6 +421,65 @@ static int check_device_error(zc_state *st) {
     return ZC_OK;
 }
 
+// Sampler host half (src/sample.rs:51-62), exactly as the reference orders
+// it: serial prefix of the chunk masses, `shots` serial draws scaled by the
+// total, ascending sort, and the routing of draws to chunks
+// (partition_point(u < cum_before[c])).
+void sample_route(const double *sums, size_t nch, uint64_t len, uint64_t shots, uint64_t seed, SampleRoute *r) {
+    std::vector<double> cum(nch + 1);
+    cum[0] = 0.0;
+    for (size_t c = 0; c < nch; c++) cum[c + 1] = cum[c] + sums[c];
+    const double total = cum[nch];
+    Xoshiro rng(seed);
+    r->us.resize(shots);
+    for (uint64_t i = 0; i < shots; i++) r->us[i] = rng.f64() * total;
+    std::sort(r->us.begin(), r->us.end());
+    r->touched.clear();
+    size_t prev = std::lower_bound(r->us.begin(), r->us.end(), cum[0]) - r->us.begin();
+    for (size_t c = 0; c < nch; c++) {
+        const size_t next = std::lower_bound(r->us.begin(), r->us.end(), cum[c + 1]) - r->us.begin();
+        if (prev < next) r->touched.push_back(SampleChunk{c, prev, next, cum[c]});
+        prev = next;
+    }
+    r->chunk_len = len < (1ull << kSampleChunkLog2) ? len : (1ull << kSampleChunkLog2);
+}
+
+static size_t up256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+size_t sample_pass2_bytes(const zc_state *st, const SampleRoute &r) {
+    return up256(r.us.size() * sizeof(uint64_t)) + up256(r.us.size() * sizeof(double)) +
+           up256(r.touched.size() * sizeof(SampleChunk)) + sample_scan_scratch(r.touched.size(), r.chunk_len, exact(st));
+}
+
+// Pass 2, asynchronous. d_work (sample_pass2_bytes(st, r) bytes, 256-aligned)
+// holds [indices | draws | touched chunks | rescan scratch]; draws and chunk
+// lists small enough travel through the pinned parameter ring, larger ones
+// are copied from pageable memory (which waits for the stream).
+int sample_launch_pass2(zc_state *st, const SampleRoute &r, char *d_work, uint64_t **d_out) {
+    const size_t shots = r.us.size();
+    uint64_t *out = (uint64_t *)d_work;
+    *d_out = out;
+    if (shots == 0) return ZC_OK;
+    const size_t out_b = up256(shots * sizeof(uint64_t)), us_b = up256(shots * sizeof(double));
+    const size_t cs_b = up256(r.touched.size() * sizeof(SampleChunk));
+    const size_t cs_n = r.touched.size() * sizeof(SampleChunk);
+    const void *d_us = d_work + out_b, *d_cs = d_work + out_b + us_b;
+    int rc = ZC_OK;
+    if (shots * sizeof(double) + cs_n <= st->arena.cap / 4) {
+        rc = arena_put(st, r.us.data(), shots * sizeof(double), &d_us);
+        if (rc == ZC_OK && cs_n) rc = arena_put(st, r.touched.data(), cs_n, &d_cs);
+        if (rc) return rc;
+    } else {
+        ZC_CUDA(cudaMemcpyAsync((void *)d_us, r.us.data(), shots * sizeof(double), cudaMemcpyHostToDevice, st->stream));
+        if (cs_n)
+            ZC_CUDA(cudaMemcpyAsync((void *)d_cs, r.touched.data(), cs_n, cudaMemcpyHostToDevice, st->stream));
+    }
+    ZC_CUDA(cudaMemsetAsync(out, 0, shots * sizeof(uint64_t), st->stream));
+    char *scratch = d_work + out_b + us_b + cs_b;
+    return launch_sample_scan(st, (const SampleChunk *)d_cs, r.touched.size(), (const double *)d_us, out, r.chunk_len,
+                              exact(st), scratch);
+}
+
 }  // namespace zc
 
 using namespace zc;
@@ -624,8 +683,7 @@ int zc_norm_sqr(zc_state *st, double *out) {
 }
 
 // Backend::sample: pass 1 (chunk masses) and pass 2 (per-chunk rescans) run
-// on the GPU; the serial prefix, the serial draws, the sort and the routing
-// (src/sample.rs:51-62) run on the host, exactly as the reference orders them.
+// on the GPU, the routing between them on the host.
 int zc_sample(zc_state *st, uint64_t shots, uint64_t seed, uint64_t *out) {
     if (!st) return fail(ZC_ERR_INVALID, "null state");
     if (shots == 0) return ZC_OK;
@@ -638,39 +696,14 @@ int zc_sample(zc_state *st, uint64_t shots, uint64_t seed, uint64_t *out) {
     std::vector<double> sums(nch);
     ZC_CUDA(cudaMemcpyAsync(sums.data(), st->d_part, nch * sizeof(double), cudaMemcpyDeviceToHost, st->stream));
     ZC_CUDA(cudaStreamSynchronize(st->stream));
-    std::vector<double> cum(nch + 1);
-    cum[0] = 0.0;
-    for (size_t c = 0; c < nch; c++) cum[c + 1] = cum[c] + sums[c];
-    const double total = cum[nch];
-    Xoshiro rng(seed);
-    std::vector<double> us(shots);
-    for (uint64_t i = 0; i < shots; i++) us[i] = rng.f64() * total;
-    std::sort(us.begin(), us.end());
-    std::vector<SampleChunk> touched;
-    size_t prev = std::lower_bound(us.begin(), us.end(), cum[0]) - us.begin();
-    for (size_t c = 0; c < nch; c++) {
-        const size_t next = std::lower_bound(us.begin(), us.end(), cum[c + 1]) - us.begin();
-        if (prev < next) touched.push_back(SampleChunk{c, prev, next, cum[c]});
-        prev = next;
-    }
-    const uint64_t chunk_len = st->len < (1ull << kSampleChunkLog2) ? st->len : (1ull << kSampleChunkLog2);
-    const size_t us_b = shots * sizeof(double), out_b = shots * sizeof(uint64_t);
-    const size_t cs_b = (touched.size() * sizeof(SampleChunk) + 255) & ~(size_t)255;
-    const size_t sc_b = sample_scan_scratch(touched.size(), chunk_len, exact(st));
-    rc = grow(&st->d_samp, &st->samp_cap, us_b + out_b + cs_b + sc_b + 64);
+    SampleRoute route;
+    sample_route(sums.data(), nch, st->len, shots, seed, &route);
+    rc = grow(&st->d_samp, &st->samp_cap, sample_pass2_bytes(st, route));
     if (rc) return rc;
-    char *base = (char *)st->d_samp;
-    double *d_us = (double *)base;
-    uint64_t *d_out = (uint64_t *)(base + us_b);
-    SampleChunk *d_cs = (SampleChunk *)(base + us_b + out_b);
-    void *d_scratch = base + us_b + out_b + cs_b;
-    ZC_CUDA(cudaMemcpyAsync(d_us, us.data(), us_b, cudaMemcpyHostToDevice, st->stream));
-    ZC_CUDA(cudaMemsetAsync(d_out, 0, out_b, st->stream));
-    if (!touched.empty())
-        ZC_CUDA(cudaMemcpyAsync(d_cs, touched.data(), cs_b, cudaMemcpyHostToDevice, st->stream));
-    rc = launch_sample_scan(st, d_cs, touched.size(), d_us, d_out, chunk_len, exact(st), d_scratch);
+    uint64_t *d_out = nullptr;
+    rc = sample_launch_pass2(st, route, (char *)st->d_samp, &d_out);
     if (rc) return rc;
-    ZC_CUDA(cudaMemcpyAsync(out, d_out, out_b, cudaMemcpyDeviceToHost, st->stream));
+    ZC_CUDA(cudaMemcpyAsync(out, d_out, shots * sizeof(uint64_t), cudaMemcpyDeviceToHost, st->stream));
     ZC_CUDA(cudaStreamSynchronize(st->stream));
     return ZC_OK;
 }

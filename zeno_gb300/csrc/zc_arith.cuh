@@ -123,6 +123,29 @@ __device__ __forceinline__ float2 df_from_f64(double x) {
     return make_float2(hi, lo);
 }
 
+// Exact f32 -> f64 widening with integer operations only (the FP64 pipe's
+// conversion shares its slow issue rate). Subnormals are normalised; inf and
+// NaN keep their class.
+__device__ __forceinline__ double f32_to_f64_exact(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned long long sign = (unsigned long long)(u >> 31) << 63;
+    const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+    unsigned long long bits;
+    if (e == 0xffu) {
+        bits = sign | (0x7ffull << 52) | ((unsigned long long)m << 29);
+    } else if (e != 0u) {
+        bits = sign | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29);
+    } else if (m == 0u) {
+        bits = sign;
+    } else {
+        const int sh = __clz(m) - 8;  // brings the leading one to bit 23
+        bits = sign | ((unsigned long long)(897 - sh) << 52) | ((unsigned long long)((m << sh) & 0x7fffffu) << 29);
+    }
+    return __longlong_as_double((long long)bits);
+}
+__device__ __forceinline__ double widen(double x) { return x; }
+__device__ __forceinline__ double widen(float x) { return f32_to_f64_exact(x); }
+
 // (hi, lo) -> f64 with |lo| <= ulp(hi): 53-bit integer sum, truncated.
 __device__ __forceinline__ double df_to_f64(float2 v) {
     const unsigned hb = __float_as_uint(v.x);

@@ -118,8 +118,8 @@ int launch_collapse(zc_state *st, uint32_t q, int outcome, double scale64);
 // f64 partial sums of |amp|^2 over chunks of 2^16 (exact: serial within a
 // chunk in the reference's order; otherwise parallel double-float).
 // mode 0: all amplitudes (norm / sampler pass 1); mode 1: the q=1 half of
-// qubit q (prob_one). Writes nchunks partials to st->d_part.
-int launch_chunk_sums(zc_state *st, int mode, uint32_t q, size_t *nchunks, bool exact);
+// qubit q (prob_one). Writes nchunks partials to `out` (default st->d_part).
+int launch_chunk_sums(zc_state *st, int mode, uint32_t q, size_t *nchunks, bool exact, double *out = nullptr);
 // Sum of st->d_part[0..nchunks) into st->d_scalar (exact: serial, in order).
 int launch_serial_sum(zc_state *st, size_t nchunks, bool exact);
 // Sampler pass 2 (sample.rs:64-108): a touched chunk and its draws.
@@ -156,5 +156,14 @@ int launch_trajectories(zc_state *st, uint32_t n, const TrajOp *d_ops, int nops,
 int launch_sample_scan(zc_state *st, const SampleChunk *d_chunks, size_t nchunks, const double *d_us,
                        uint64_t *d_out, uint64_t chunk_len, bool exact, void *d_scratch);
 size_t sample_scan_scratch(size_t nchunks, uint64_t chunk_len, bool exact);
+// Sampler phases, so a caller can sample many states with two syncs.
+struct SampleRoute {
+    std::vector<double> us;            // sorted scaled draws
+    std::vector<SampleChunk> touched;  // chunks that received draws
+    uint64_t chunk_len = 0;
+};
+void sample_route(const double *sums, size_t nch, uint64_t len, uint64_t shots, uint64_t seed, SampleRoute *r);
+size_t sample_pass2_bytes(const zc_state *st, const SampleRoute &r);
+int sample_launch_pass2(zc_state *st, const SampleRoute &r, char *d_work, uint64_t **d_out);
 
 }  // namespace zc

@@ -106,7 +106,7 @@ __global__ void __launch_bounds__(kChainThreads) k_chain(const T *__restrict__ r
                     }
 #pragma unroll
                     for (int u = 0; u < 8; u++)
-                        if (r0 + u < R) buf[(r0 + u) * kRowPad + lane] = p2((double)vr[u], (double)vi[u]);
+                        if (r0 + u < R) buf[(r0 + u) * kRowPad + lane] = p2(widen(vr[u]), widen(vi[u]));
                 }
             }
             nb_arrive(bar_full(p), 64);
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(128) k_resolve(const T *__restrict__ re, const
         const uint64_t e1 = e0 + kStageElems < len ? e0 + kStageElems : len;
         uint64_t res = ~0ull;
         for (uint64_t e = e0; e < e1; e++) {
-            acc = radd(acc, p2((double)re[first + e], (double)im[first + e]));
+            acc = radd(acc, p2(widen(re[first + e]), widen(im[first + e])));
             if (uk < dkey(acc)) {
                 res = first + e;
                 break;
@@ -414,34 +414,34 @@ int run_chain(zc_state *st, unsigned blocks, uint64_t total, uint64_t chunk, uin
 
 }  // namespace
 
-int launch_chunk_sums(zc_state *st, int mode, uint32_t q, size_t *nchunks_out, bool exact) {
+int launch_chunk_sums(zc_state *st, int mode, uint32_t q, size_t *nchunks_out, bool exact, double *out) {
     const uint64_t total = mode == 0 ? st->len : st->len / 2;
     const uint64_t chunk = total < (1ull << kSampleChunkLog2) ? total : (1ull << kSampleChunkLog2);
     const uint64_t nch = (total + chunk - 1) / chunk;
-    if (nch > st->part_cap) {
+    if (!out && nch > st->part_cap) {
         if (st->d_part) cudaFree(st->d_part);
         st->d_part = nullptr;
         ZC_CUDA(cudaMalloc(&st->d_part, nch * sizeof(double)));
         st->part_cap = nch;
     }
+    double *part = out ? out : st->d_part;
     ProfScope ps(st, K_CHUNK_SUMS, (mode == 0 ? 1.0 : 0.5) * st->len * (st->prec / 8) * 2);
     st->ctr.launches++;
     *nchunks_out = nch;
     if (!exact) {
         if (st->prec == 64)
             k_chunk_sums_df<double><<<(unsigned)nch, kDfThreads, 0, st->stream>>>(
-                (const double *)st->re, (const double *)st->im, total, chunk, mode, q, st->d_part);
+                (const double *)st->re, (const double *)st->im, total, chunk, mode, q, part);
         else
             k_chunk_sums_df<float><<<(unsigned)nch, kDfThreads, 0, st->stream>>>(
-                (const float *)st->re, (const float *)st->im, total, chunk, mode, q, st->d_part);
+                (const float *)st->re, (const float *)st->im, total, chunk, mode, q, part);
         ZC_CUDA(cudaGetLastError());
         return ZC_OK;
     }
     const unsigned blocks = (unsigned)((nch + 31) / 32);
     if (st->prec == 64)
-        return run_chain<double, false>(st, blocks, total, chunk, nch, mode, q, nullptr, nullptr, st->d_part, nullptr,
-                                        0);
-    return run_chain<float, false>(st, blocks, total, chunk, nch, mode, q, nullptr, nullptr, st->d_part, nullptr, 0);
+        return run_chain<double, false>(st, blocks, total, chunk, nch, mode, q, nullptr, nullptr, part, nullptr, 0);
+    return run_chain<float, false>(st, blocks, total, chunk, nch, mode, q, nullptr, nullptr, part, nullptr, 0);
 }
 
 int launch_serial_sum(zc_state *st, size_t nchunks, bool exact) {

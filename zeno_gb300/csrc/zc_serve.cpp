@@ -36,6 +36,7 @@ namespace {
 constexpr uint64_t kServeMaxShots = 65536;
 constexpr uint32_t kServeMaxQubits = 30;
 constexpr size_t kBlobBytes = 16u << 20;
+constexpr int kRounds = 4;  // packed launches per precision per step (one host blob each)
 
 struct Request {
     uint64_t id = 0;
@@ -50,7 +51,7 @@ struct Request {
 };
 
 struct Group {  // one precision: its packed-launch graph and blob buffers
-    char *h_blob = nullptr;
+    char *h_blob[kRounds] = {};
     char *d_blob = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -73,7 +74,17 @@ struct zc_server {
     std::vector<zc::Request *> active;
     std::map<uint64_t, zc::Request *> done;
     zc::Group groups[2];  // [0] f32, [1] f64
+    // batched sampling of a step's finished requests
+    double *d_bpart = nullptr, *h_bpart = nullptr;
+    size_t bpart_cap = 0, hbpart_cap = 0;
+    char *d_bwork = nullptr;
+    size_t bwork_cap = 0;
+    uint64_t *h_bout = nullptr;
+    size_t hbout_cap = 0;
     uint64_t launches = 0, packed_launches = 0, admitted = 0, completed = 0;
+    uint64_t steps = 0, plan_us = 0, sample_us = 0, wait_us = 0;
+    double device_ms = 0.0;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
 
 namespace zc {
@@ -109,8 +120,8 @@ void pool_free(zc_server *s, size_t off, size_t bytes) {
     }
 }
 
-// A state view over pool memory that borrows the server context's stream,
-// arena and reduction scratch (so sampling allocates nothing).
+// A state view over pool memory that borrows the server context's stream
+// and parameter ring.
 void make_view(zc_server *s, Request *r) {
     zc_state &v = r->view;
     const zc_state *c = s->ctx;
@@ -125,12 +136,12 @@ void make_view(zc_server *s, Request *r) {
     v.re = s->pool + r->off;
     v.im = s->pool + r->off + half;
     v.arena = c->arena;
-    v.d_part = c->d_part;
-    v.part_cap = c->part_cap;
+    v.d_part = nullptr;  // the server samples with its own batch buffers
+    v.part_cap = 0;
     v.d_scalar = c->d_scalar;
     v.h_scalar = c->h_scalar;
-    v.d_samp = c->d_samp;
-    v.samp_cap = c->samp_cap;
+    v.d_samp = nullptr;
+    v.samp_cap = 0;
     v.d_err = c->d_err;
     v.name = r->prec == 64 ? "cuda-f64" : "cuda-f32";
 }
@@ -146,7 +157,7 @@ int capture_group(zc_server *s, int gi) {
     Group &g = s->groups[gi];
     cudaStream_t st = s->ctx->stream;
     ZC_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    cudaMemcpyAsync(g.d_blob, g.h_blob, sizeof(SweepBatch), cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(g.d_blob, g.h_blob[0], sizeof(SweepBatch), cudaMemcpyHostToDevice, st);
     int rc = launch_sweep_multi(st, s->ctx->num_sms, gi ? 64 : 32, (s->flags & ZC_FLAG_FAST) == 0, g.d_blob,
                                 s->ctx->d_err);
     cudaError_t e = cudaStreamEndCapture(st, &g.graph);
@@ -166,8 +177,10 @@ int capture_group(zc_server *s, int gi) {
     return ZC_OK;
 }
 
-// Build and launch the packed sweep of every active request of one precision.
-int packed_step(zc_server *s, int gi) {
+// Build and launch the packed sweep of every active request of one precision
+// (round `round` of the step: its host blob stays untouched until the step's
+// final sync). *issued counts the launches made.
+int packed_step(zc_server *s, int gi, int round, int *issued) {
     Group &g = s->groups[gi];
     const int prec = gi ? 64 : 32;
     const bool ex = (s->flags & ZC_FLAG_FAST) == 0;
@@ -189,6 +202,7 @@ int packed_step(zc_server *s, int gi) {
             if (rc) return rc;
             r->queue.erase(r->queue.begin());
             s->launches++;
+            (*issued)++;
             continue;
         }
         SweepJob j{};
@@ -222,27 +236,103 @@ int packed_step(zc_server *s, int gi) {
         j.tables_off += body_off;
     }
     SweepBatch hdr{(uint32_t)jobs.size(), 0, tiles};
-    memcpy(g.h_blob, &hdr, sizeof hdr);
-    memcpy(g.h_blob + sizeof hdr, jobs.data(), jobs.size() * sizeof(SweepJob));
-    memcpy(g.h_blob + body_off, body.data(), body.size());
+    char *hb = g.h_blob[round];
+    memcpy(hb, &hdr, sizeof hdr);
+    memcpy(hb + sizeof hdr, jobs.data(), jobs.size() * sizeof(SweepJob));
+    memcpy(hb + body_off, body.data(), body.size());
     if (!g.exec && g.graph == nullptr && g.launches > 0) {
         int rc = capture_group(s, gi);
         if (rc) return rc;
     }
     if (g.exec) {
-        ZC_CUDA(cudaGraphExecMemcpyNodeSetParams1D(g.exec, g.copy_node, g.d_blob, g.h_blob, total,
-                                                   cudaMemcpyHostToDevice));
+        ZC_CUDA(cudaGraphExecMemcpyNodeSetParams1D(g.exec, g.copy_node, g.d_blob, hb, total, cudaMemcpyHostToDevice));
         ZC_CUDA(cudaGraphLaunch(g.exec, s->ctx->stream));
     } else {
         // first packed launch of the server runs uncaptured (kernel attributes get set here)
-        ZC_CUDA(cudaMemcpyAsync(g.d_blob, g.h_blob, total, cudaMemcpyHostToDevice, s->ctx->stream));
+        ZC_CUDA(cudaMemcpyAsync(g.d_blob, hb, total, cudaMemcpyHostToDevice, s->ctx->stream));
         int rc = launch_sweep_multi(s->ctx->stream, s->ctx->num_sms, prec, ex, g.d_blob, s->ctx->d_err);
         if (rc) return rc;
     }
     s->launches++;
     s->packed_launches++;
     g.launches++;
+    (*issued)++;
     for (auto &pr : planned) erase_taken(pr.first->queue, pr.second.taken);
+    return ZC_OK;
+}
+
+// Grow a device or pinned host buffer to at least `need` bytes (contents dropped).
+int grow_dev(void **p, size_t *cap, size_t need) {
+    if (need <= *cap) return ZC_OK;
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    *cap = 0;
+    ZC_CUDA(cudaMalloc(p, need));
+    *cap = need;
+    return ZC_OK;
+}
+int grow_host(void **p, size_t *cap, size_t need) {
+    if (need <= *cap) return ZC_OK;
+    if (*p) cudaFreeHost(*p);
+    *p = nullptr;
+    *cap = 0;
+    ZC_CUDA(cudaMallocHost(p, need));
+    *cap = need;
+    return ZC_OK;
+}
+
+// Sample every finished request of a step with two device syncs in total:
+// all chunk-mass passes, one copy back; host routing per request; all
+// rescans, one copy of every index list back. Per request this is exactly
+// zc_sample (same kernels, same order, same seed stream).
+int sample_finished(zc_server *s, const std::vector<Request *> &fin) {
+    zc_state *c = s->ctx;
+    const bool ex = (s->flags & ZC_FLAG_FAST) == 0;
+    std::vector<size_t> part_off(fin.size()), nch(fin.size());
+    size_t tot_ch = 0;
+    for (size_t i = 0; i < fin.size(); i++) {
+        const uint64_t len = 1ull << fin[i]->n;
+        const uint64_t chunk = len < (1ull << kSampleChunkLog2) ? len : (1ull << kSampleChunkLog2);
+        nch[i] = (size_t)((len + chunk - 1) / chunk);
+        part_off[i] = tot_ch;
+        tot_ch += nch[i];
+    }
+    if (tot_ch == 0) return ZC_OK;
+    int rc = grow_dev((void **)&s->d_bpart, &s->bpart_cap, tot_ch * sizeof(double));
+    if (rc == ZC_OK) rc = grow_host((void **)&s->h_bpart, &s->hbpart_cap, tot_ch * sizeof(double));
+    if (rc) return rc;
+    for (size_t i = 0; i < fin.size(); i++) {
+        size_t n = 0;
+        if ((rc = launch_chunk_sums(&fin[i]->view, 0, 0, &n, ex, s->d_bpart + part_off[i]))) return rc;
+    }
+    ZC_CUDA(cudaMemcpyAsync(s->h_bpart, s->d_bpart, tot_ch * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    ZC_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<SampleRoute> routes(fin.size());
+    std::vector<size_t> work_off(fin.size()), out_off(fin.size());
+    size_t tot_work = 0, tot_out = 0;
+    for (size_t i = 0; i < fin.size(); i++) {
+        Request *r = fin[i];
+        sample_route(s->h_bpart + part_off[i], nch[i], 1ull << r->n, r->shots, splitmix64(r->seed), &routes[i]);
+        work_off[i] = tot_work;
+        tot_work += (sample_pass2_bytes(&r->view, routes[i]) + 255) & ~(size_t)255;
+        out_off[i] = tot_out;
+        tot_out += r->shots;
+    }
+    if ((rc = grow_dev((void **)&s->d_bwork, &s->bwork_cap, tot_work))) return rc;
+    if ((rc = grow_host((void **)&s->h_bout, &s->hbout_cap, tot_out * sizeof(uint64_t)))) return rc;
+    for (size_t i = 0; i < fin.size(); i++) {
+        Request *r = fin[i];
+        uint64_t *d_out = nullptr;
+        r->view.arena = c->arena;  // the view shares the server's parameter ring
+        rc = sample_launch_pass2(&r->view, routes[i], s->d_bwork + work_off[i], &d_out);
+        c->arena = r->view.arena;
+        if (rc) return rc;
+        ZC_CUDA(cudaMemcpyAsync(s->h_bout + out_off[i], d_out, r->shots * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+                                c->stream));
+    }
+    ZC_CUDA(cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < fin.size(); i++)
+        fin[i]->result.assign(s->h_bout + out_off[i], s->h_bout + out_off[i] + fin[i]->shots);
     return ZC_OK;
 }
 
@@ -288,23 +378,13 @@ int zc_server_create(const zc_server_options *opt, zc_server **out) {
     cudaError_t e = cudaMalloc(&s->pool, s->pool_bytes);
     if (e != cudaSuccess) return bail(fail(ZC_ERR_MEMORY, "server pool allocation failed"));
     s->free_list.push_back({0, s->pool_bytes});
-    // reduction / sampler scratch sized for the largest admissible request
-    zc_state *c = s->ctx;
-    const size_t chunks = ((size_t)1 << kServeMaxQubits) >> kSampleChunkLog2;
-    cudaFree(c->d_part);
-    c->d_part = nullptr;
-    if ((e = cudaMalloc(&c->d_part, chunks * sizeof(double))) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc"));
-    c->part_cap = chunks;
-    const size_t touched_max = std::min<size_t>(kServeMaxShots, chunks);
-    const size_t samp = kServeMaxShots * (sizeof(double) + sizeof(uint64_t)) +
-                        ((kServeMaxShots * sizeof(SampleChunk) + 255) & ~(size_t)255) +
-                        sample_scan_scratch(touched_max, (size_t)1 << kSampleChunkLog2, (s->flags & ZC_FLAG_FAST) == 0) + 64;
-    if ((e = cudaMalloc(&c->d_samp, samp)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc"));
-    c->samp_cap = samp;
     for (auto &g : s->groups) {
-        if ((e = cudaMallocHost(&g.h_blob, kBlobBytes)) != cudaSuccess) return bail(cuda_fail(e, "cudaMallocHost"));
+        for (auto &hb : g.h_blob)
+            if ((e = cudaMallocHost(&hb, kBlobBytes)) != cudaSuccess) return bail(cuda_fail(e, "cudaMallocHost"));
         if ((e = cudaMalloc(&g.d_blob, kBlobBytes)) != cudaSuccess) return bail(cuda_fail(e, "cudaMalloc"));
     }
+    if ((e = cudaEventCreate(&s->ev0)) != cudaSuccess || (e = cudaEventCreate(&s->ev1)) != cudaSuccess)
+        return bail(cuda_fail(e, "cudaEventCreate"));
     *out = s;
     return ZC_OK;
 }
@@ -318,10 +398,17 @@ void zc_server_destroy(zc_server *s) {
     for (auto &g : s->groups) {
         if (g.exec) cudaGraphExecDestroy(g.exec);
         if (g.graph) cudaGraphDestroy(g.graph);
-        if (g.h_blob) cudaFreeHost(g.h_blob);
+        for (auto hb : g.h_blob)
+            if (hb) cudaFreeHost(hb);
         if (g.d_blob) cudaFree(g.d_blob);
     }
+    if (s->d_bpart) cudaFree(s->d_bpart);
+    if (s->h_bpart) cudaFreeHost(s->h_bpart);
+    if (s->d_bwork) cudaFree(s->d_bwork);
+    if (s->h_bout) cudaFreeHost(s->h_bout);
     if (s->pool) cudaFree(s->pool);
+    if (s->ev0) cudaEventDestroy(s->ev0);
+    if (s->ev1) cudaEventDestroy(s->ev1);
     zc_destroy(s->ctx);
     delete s;
 }
@@ -376,25 +463,49 @@ int zc_server_step(zc_server *s, zc_server_status *status) {
         s->admitted++;
         s->launches++;
     }
-    // 2. one packed launch per precision (plus lone launches for dense blocks)
-    for (int gi = 0; gi < 2 && rc == ZC_OK; gi++) rc = packed_step(s, gi);
-    if (rc) return rc;
-    // 3. completions: sample, free the slot
-    std::vector<Request *> still;
+    using clk = std::chrono::steady_clock;
+    auto us_since = [](clk::time_point t) {
+        return (uint64_t)std::chrono::duration_cast<std::chrono::microseconds>(clk::now() - t).count();
+    };
+    // 2. up to kRounds packed launches per precision (plus lone launches for
+    //    dense blocks), queued back to back without a host sync in between
+    ZC_CUDA(cudaEventRecord(s->ev0, s->ctx->stream));
+    auto t0 = clk::now();
+    for (int round = 0; round < kRounds; round++) {
+        int issued = 0;
+        for (int gi = 0; gi < 2 && rc == ZC_OK; gi++) rc = packed_step(s, gi, round, &issued);
+        if (rc) return rc;
+        if (!issued) break;
+    }
+    s->plan_us += us_since(t0);
+    // 3. completions: sample all finished requests together, free their slots
+    t0 = clk::now();
+    std::vector<Request *> still, fin, sampled;
     for (Request *r : s->active) {
         if (!r->queue.empty()) {
             still.push_back(r);
             continue;
         }
-        r->result.assign(r->shots, 0);
-        if (!r->finals.empty() && r->shots && (rc = zc_sample(&r->view, r->shots, splitmix64(r->seed), r->result.data())))
-            return rc;
+        fin.push_back(r);
+        if (!r->finals.empty() && r->shots) sampled.push_back(r);
+        else r->result.assign(r->shots, 0);
+    }
+    if ((rc = sample_finished(s, sampled))) return rc;
+    for (Request *r : fin) {
         pool_free(s, r->off, r->bytes);
         s->done[r->id] = r;
         s->completed++;
     }
     s->active.swap(still);
+    s->sample_us += us_since(t0);
+    ZC_CUDA(cudaEventRecord(s->ev1, s->ctx->stream));
+    t0 = clk::now();
     ZC_CUDA(cudaStreamSynchronize(s->ctx->stream));
+    s->wait_us += us_since(t0);
+    float ms = 0.f;
+    ZC_CUDA(cudaEventElapsedTime(&ms, s->ev0, s->ev1));
+    s->device_ms += ms;
+    s->steps++;
     int h = 0;
     ZC_CUDA(cudaMemcpy(&h, s->ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
     if (h) return fail(ZC_ERR_CUDA, "packed sweep gave up waiting for a bulk copy");
@@ -409,6 +520,11 @@ int zc_server_step(zc_server *s, zc_server_status *status) {
         size_t free_b = 0;
         for (auto &f : s->free_list) free_b += f.second;
         status->pool_used = s->pool_bytes - free_b;
+        status->steps = s->steps;
+        status->plan_us = s->plan_us;
+        status->sample_us = s->sample_us;
+        status->wait_us = s->wait_us;
+        status->device_us = (uint64_t)(s->device_ms * 1e3);
     }
     return ZC_OK;
 }

@@ -490,18 +490,25 @@ __global__ void __launch_bounds__(kSweepThreads, kSweepCtasPerSm)
     sweep_init(c);
     uint32_t phase = 0;
     int cur = -1;
+    // Tiles go to CTAs round-robin (concurrent tiles stay adjacent in memory
+    // and big and small jobs mix evenly); the job is looked up only when a
+    // tile falls outside the current one.
+    uint64_t job_lo = 1, job_hi = 0;
     for (uint64_t t = blockIdx.x; t < total; t += gridDim.x) {
-        uint32_t lo = 0, hi = njobs;  // last job with tile_start <= t
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) / 2;
-            if (jobs[mid].tile_start <= t) lo = mid;
-            else hi = mid;
-        }
-        const SweepJob &J = jobs[lo];
-        if ((int)lo != cur) {
-            load_job(c, reinterpret_cast<const MicroOp *>(blob + J.ops_off), (int)J.nops, J.L, J.H, J.hpos);
+        if (t < job_lo || t >= job_hi) {
+            uint32_t lo = 0, hi = njobs;  // last job with tile_start <= t
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) / 2;
+                if (jobs[mid].tile_start <= t) lo = mid;
+                else hi = mid;
+            }
+            const SweepJob &Jn = jobs[lo];
+            load_job(c, reinterpret_cast<const MicroOp *>(blob + Jn.ops_off), (int)Jn.nops, Jn.L, Jn.H, Jn.hpos);
             cur = (int)lo;
+            job_lo = Jn.tile_start;
+            job_hi = Jn.tile_start + Jn.ntiles;
         }
+        const SweepJob &J = jobs[cur];
         T *sre = reinterpret_cast<T *>(smem);
         T *sim = sre + (1u << (J.L + J.H));
         if (!process_tile(c, reinterpret_cast<T *>(J.re), reinterpret_cast<T *>(J.im), t - J.tile_start,

@@ -37,7 +37,8 @@ class ServerOptions(C.Structure):
 
 class ServerStatus(C.Structure):
     _fields_ = [(n, C.c_uint64) for n in ("pending", "active", "done", "launches", "packed_launches", "admitted",
-                                          "completed", "pool_used")]
+                                          "completed", "pool_used", "steps", "plan_us", "sample_us",
+                                          "wait_us", "device_us")]
 
 
 _bound = False
@@ -169,6 +170,7 @@ def serve_stream(reqs: List[Request], flags: int = zb.FLAG_FAST, pool_bytes: int
     i = 0
     t0 = time.perf_counter()
     done = 0
+    step_s = 0.0
     while done < len(reqs):
         now = time.perf_counter() - t0
         while i < len(pending) and pending[i].arrival <= now:
@@ -176,7 +178,9 @@ def serve_stream(reqs: List[Request], flags: int = zb.FLAG_FAST, pool_bytes: int
             q.rid = srv.submit(q.program, q.precision, q.shots, q.seed)
             by_id[q.rid] = q
             i += 1
+        ts = time.perf_counter()
         st = srv.step()
+        step_s += time.perf_counter() - ts
         for rid in srv.done_ids():
             q = by_id[rid]
             idx = srv.take(rid, q.shots)
@@ -192,6 +196,10 @@ def serve_stream(reqs: List[Request], flags: int = zb.FLAG_FAST, pool_bytes: int
     stats = _latency_stats(reqs, wall)
     stats["launches"] = srv.status.launches
     stats["packed_launches"] = srv.status.packed_launches
+    stats["steps"] = srv.status.steps
+    stats["host_s"] = {"plan_launch": srv.status.plan_us * 1e-6, "sample": srv.status.sample_us * 1e-6,
+                       "wait_device": srv.status.wait_us * 1e-6, "in_step": step_s}
+    stats["device_busy_s"] = srv.status.device_us * 1e-6
     srv.close()
     return stats
 
@@ -199,6 +207,7 @@ def serve_stream(reqs: List[Request], flags: int = zb.FLAG_FAST, pool_bytes: int
 def plain_stream(reqs: List[Request], flags: int = zb.FLAG_FAST, keep_counts: bool = False) -> Dict[str, float]:
     """One circuit per call, FIFO in arrival order (each request runs alone)."""
     t0 = time.perf_counter()
+    moved, sweeps, sim = 0, 0, 0.0
     for q in sorted(reqs, key=lambda q: q.arrival):
         now = time.perf_counter() - t0
         if q.arrival > now:
@@ -206,10 +215,16 @@ def plain_stream(reqs: List[Request], flags: int = zb.FLAG_FAST, keep_counts: bo
         shell = circ.Program(q.n, list(q.program.cregs), [])  # registers only: the program is compiled
         r = zb.run(shell, shots=q.shots, seed=q.seed, precision=q.precision, flags=flags, program=q.program)
         q.done = time.perf_counter() - t0
+        moved += r.bytes_moved
+        sweeps += r.sweeps
+        sim += r.sim_time
         if keep_counts:
             q.counts = r.counts
     wall = time.perf_counter() - t0
-    return _latency_stats(reqs, wall)
+    stats = _latency_stats(reqs, wall)
+    # state traffic of the sweeps and per-op passes (the packed server moves the same bytes)
+    stats.update(bytes_moved=moved, sweeps=sweeps, sim_seconds=sim)
+    return stats
 
 
 def _latency_stats(reqs: List[Request], wall: float) -> Dict[str, float]:

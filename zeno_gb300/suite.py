@@ -5,6 +5,8 @@
   python -m zeno_gb300.suite big        # 33q depth-40 f64 (128 GiB state)
   python -m zeno_gb300.suite serving    # request stream at several arrival rates, server vs one-per-call
   python -m zeno_gb300.suite trajectories  # 4096 noisy 16q trajectories, batched vs per-shot
+  python -m zeno_gb300.suite tc         # 28q gate mix fused to k=5..7 blocks on tensor cores vs FP64
+  python -m zeno_gb300.suite sampler    # sample / prob_one per state size, exact and fast
 
 Each prints JSON lines. Times are wall-clock around complete runs
 (`zc_run`: state allocation, ops, sampling), the semantics of zeno's
@@ -77,6 +79,10 @@ def serving(args):
         reqs = serve.request_stream(args.requests, rate=rate, master_seed=2024, n_max=args.n_max)
         serve.compile_requests(reqs)
         s = serve.serve_stream(reqs)
+        if args.server_only:
+            print(json.dumps({"workload": "serving", "rate_per_s": rate, "requests": args.requests,
+                              "qubits": [8, args.n_max], "server": s}), flush=True)
+            continue
         reqs2 = serve.request_stream(args.requests, rate=rate, master_seed=2024, n_max=args.n_max)
         for a, b in zip(reqs2, reqs):
             b_prog = b.program
@@ -134,13 +140,49 @@ def tc(args):
                       "ops": len(prog1.ops), "max_abs_damp_vs_f64": d}), flush=True)
 
 
+def sampler(args):
+    """Sampler and reductions per state size, exact and fast mode: wall time of
+    one 1024-shot sample and one prob_one, and the per-kernel device times
+    (in-library CUDA-event profiler) of two samples, one prob_one, one norm."""
+    import numpy as np
+
+    h = np.array([[1, 1], [1, -1]], dtype=complex) / np.sqrt(2)
+    for prec in (64, 32):
+        for flags, mode in ((zb.FLAG_EXACT, "exact"), (zb.FLAG_FAST, "fast")):
+            for n in args.sizes:
+                be = zb.CudaBackend(n, prec, flags)
+                for q in range(n):
+                    be.apply_unitary([q], h)
+                be.norm_sqr()
+                be.profile(True)
+                for _ in range(2):
+                    be.sample(1024, 5)
+                be.prob_one(n - 1)
+                be.norm_sqr()
+                prof = be.profile_read()
+                be.profile(False)
+                t0 = time.perf_counter()
+                be.sample(1024, 5)
+                ts = time.perf_counter() - t0
+                t0 = time.perf_counter()
+                be.prob_one(n - 1)
+                tp = time.perf_counter() - t0
+                print(json.dumps({"workload": "sampler", "qubits": n, "precision": prec, "mode": mode,
+                                  "sample_1024_ms": ts * 1e3, "prob_one_ms": tp * 1e3,
+                                  "kernels_ms": {k: [v["launches"], round(v["ms"], 3)] for k, v in prof.items()}}),
+                      flush=True)
+                be.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["qft", "fusion", "big", "serving", "trajectories", "tc"])
+    ap.add_argument("what", choices=["qft", "fusion", "big", "serving", "trajectories", "tc", "sampler"])
+    ap.add_argument("--sizes", type=int, nargs="*", default=[16, 20, 22, 26, 28, 30])
     ap.add_argument("--qubits", type=int, default=None)
     ap.add_argument("--requests", type=int, default=1000)
     ap.add_argument("--rates", type=float, nargs="*", default=[100.0, 1000.0, 10000.0])
     ap.add_argument("--n-max", type=int, default=26)
+    ap.add_argument("--server-only", action="store_true", help="serving: skip the one-circuit-per-call arm")
     a = ap.parse_args()
     if a.qubits is None:
         a.qubits = {"fusion": 30, "big": 33, "tc": 28}.get(a.what, 30)

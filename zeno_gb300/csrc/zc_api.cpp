@@ -21,7 +21,7 @@ static thread_local std::string g_err;
 
 const char *const kKernelNames[K_NKINDS] = {"1q",         "kq",         "diag1",       "diagk",    "cx",
                                             "swap",       "sweep",      "chunk_sums",  "serial_sum", "sample_scan",
-                                            "collapse",   "reset",      "trajectories"};
+                                            "collapse",   "reset",      "trajectories", "tc_block"};
 
 ProfScope::ProfScope(zc_state *s, int kind, double bytes) : st(s) {
     if (!st || !st->prof) return;
@@ -118,11 +118,13 @@ static int check_support(const zc_state *st, const uint32_t *qs, uint32_t k, uin
 
 static inline bool exact(const zc_state *st) { return (st->flags & ZC_FLAG_FAST) == 0; }
 
+static int check_device_error(zc_state *st);
+
 static int sync_read_scalar(zc_state *st, double *out) {
     ZC_CUDA(cudaMemcpyAsync(st->h_scalar, st->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, st->stream));
     ZC_CUDA(cudaStreamSynchronize(st->stream));
     *out = *st->h_scalar;
-    return ZC_OK;
+    return check_device_error(st);  // a kernel that gave up leaves a wrong state behind
 }
 
 static int grow(void **p, size_t *cap, size_t need) {
@@ -142,44 +144,13 @@ static constexpr size_t kQueueWindow = 2048;  // ops examined per sweep plan
 static constexpr size_t kQueueFlushAt = 8192; // queue length that forces a flush
 static constexpr uint32_t kMinSweepQubits = 14;
 
-// Real 2D x 2D form [[Mr, -Mi], [Mi, Mr]] of a complex D x D matrix, split
-// into TF32 parts (round to nearest, ties away: the rounding of cvt.rna.tf32).
-static float tf32_rna(float x) {
-    uint32_t u;
-    memcpy(&u, &x, 4);
-    if ((u & 0x7f800000u) != 0x7f800000u) u = (u + 0x1000u) & 0xffffe000u;
-    float r;
-    memcpy(&r, &u, 4);
-    return r;
-}
-
-static int stage_tc_matrix(zc_state *st, const double *mat, uint32_t k, const void **dev) {
-    const size_t D = (size_t)1 << k, R = 2 * D;
-    std::vector<float> a(2 * R * R);
-    float *ah = a.data(), *al = a.data() + R * R;
-    for (size_t r = 0; r < R; r++)
-        for (size_t c = 0; c < R; c++) {
-            const size_t i = r % D, j = c % D;
-            const double mr = mat[2 * (i * D + j)], mi = mat[2 * (i * D + j) + 1];
-            const double v = (r < D) == (c < D) ? mr : (r < D ? -mi : mi);
-            const float h = tf32_rna((float)v);
-            ah[r * R + c] = h;
-            al[r * R + c] = tf32_rna((float)(v - (double)h));
-        }
-    return arena_put(st, a.data(), a.size() * sizeof(float), dev);
-}
-
 int launch_single(zc_state *st, const QOp &op) {
     const bool ex = exact(st);
     switch (op.kind) {
         case Q_UNITARY: {
             if (op.k == 1) return launch_1q(st, op.qs[0], op.data.data(), ex);
-            if (op.k >= 3 && st->prec == 32 && (st->flags & ZC_FLAG_TENSOR)) {
-                const void *dev = nullptr;
-                int rc = stage_tc_matrix(st, op.data.data(), op.k, &dev);
-                if (rc) return rc;
-                return launch_block_tc(st, op.qs, op.k, (const float *)dev);
-            }
+            if (op.k >= 3 && st->prec == 32 && (st->flags & ZC_FLAG_TENSOR))
+                return launch_block_tc(st, op.qs, op.k, op.data.data());
             const void *dev = nullptr;
             int rc = stage_table(st, op.data.data(), (size_t)1 << (2 * op.k), &dev);
             if (rc) return rc;
@@ -410,6 +381,8 @@ static int check_device_error(zc_state *st) {
     ZC_CUDA(cudaStreamSynchronize(st->stream));
     if (h[0]) {
         cudaMemsetAsync(st->d_err, 0, sizeof(h), st->stream);
+        if (h[0] == 3)
+            return fail(ZC_ERR_CUDA, "tensor-core block kernel gave up waiting for a copy or an MMA (device wait limit)");
         char buf[320];
         snprintf(buf, sizeof(buf),
                  "sweep kernel %s (cta %d tile %d phase %d barrier %08x%08x L %d H %d ops %d tiles done %d index %08x)",
@@ -705,7 +678,7 @@ int zc_sample(zc_state *st, uint64_t shots, uint64_t seed, uint64_t *out) {
     if (rc) return rc;
     ZC_CUDA(cudaMemcpyAsync(out, d_out, shots * sizeof(uint64_t), cudaMemcpyDeviceToHost, st->stream));
     ZC_CUDA(cudaStreamSynchronize(st->stream));
-    return ZC_OK;
+    return check_device_error(st);
 }
 
 int zc_statevector(zc_state *st, double *out) {
@@ -717,6 +690,7 @@ int zc_statevector(zc_state *st, double *out) {
     ZC_CUDA(cudaMemcpyAsync(re.data(), st->re, st->len * es, cudaMemcpyDeviceToHost, st->stream));
     ZC_CUDA(cudaMemcpyAsync(im.data(), st->im, st->len * es, cudaMemcpyDeviceToHost, st->stream));
     ZC_CUDA(cudaStreamSynchronize(st->stream));
+    if ((rc = check_device_error(st))) return rc;
     for (size_t i = 0; i < st->len; i++) {
         if (st->prec == 64) {
             out[2 * i] = ((double *)re.data())[i];

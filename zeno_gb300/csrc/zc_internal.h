@@ -44,7 +44,7 @@ struct Launch {
 // Kernel classes for the per-launch profiler (zc_profile / zc_profile_read).
 enum : int {
     K_1Q = 0, K_KQ, K_DIAG1, K_DIAGK, K_CX, K_SWAP, K_SWEEP, K_CHUNK_SUMS, K_SERIAL_SUM, K_SAMPLE_SCAN,
-    K_COLLAPSE, K_RESET, K_TRAJ, K_NKINDS
+    K_COLLAPSE, K_RESET, K_TRAJ, K_TC, K_NKINDS
 };
 extern const char *const kKernelNames[K_NKINDS];
 
@@ -107,8 +107,9 @@ struct ProfScope {
 
 int launch_1q(zc_state *st, uint32_t q, const double *m8, bool exact);
 int launch_kq(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat, bool exact);
-// Dense k-qubit block (k = 3..7) on tensor cores, f32 state, 3xTF32 (zc_tc.cu).
-int launch_block_tc(zc_state *st, const uint32_t *qs, uint32_t k, const float *dev_a);
+// Dense k-qubit block (k = 3..7) on tensor cores, f32 state, 3xTF32 (zc_tc.cu);
+// mat: row-major 2^k x 2^k complex (interleaved f64 pairs).
+int launch_block_tc(zc_state *st, const uint32_t *qs, uint32_t k, const double *mat);
 int launch_diag1(zc_state *st, uint32_t q, const double *d4, bool exact);
 int launch_diagk(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_diag, bool exact);
 int launch_cx(zc_state *st, uint32_t c, uint32_t t);

@@ -110,33 +110,68 @@ def trajectories(args):
                       "launches": r.launches, "keys": len(r.counts)}), flush=True)
 
 
+def _apply_ops(be, prog):
+    for op in prog.ops:
+        if op.kind == zb.OP_UNITARY:
+            be.apply_unitary(list(op.qubits), op.data.reshape(1 << len(op.qubits), -1))
+        elif op.kind == zb.OP_DIAG:
+            be.apply_diagonal(list(op.qubits), op.data)
+        elif op.kind == zb.OP_CX:
+            be.apply_cx(op.a, op.b)
+        else:
+            be.apply_swap(op.a, op.b)
+
+
 def tc(args):
     """28q depth-60 gate mix fused to 5/6/7-qubit blocks on tensor cores (f32,
-    3xTF32) against the FP64 plain run on the GPU (exact mode = oracle bits)."""
+    3xTF32) against the FP64 plain run on the GPU: accuracy from full runs,
+    device time per kernel class from the in-library profiler."""
     import numpy as np
 
     n = args.qubits
     p = C.mixed_circuit(n, 60, 7).to_program()
     ref_prog = zb.compile(p, 1)
     ref = zb.run(p, shots=0, seed=1, precision=64, flags=zb.FLAG_FAST, statevector=True, program=ref_prog)
+    S = 2.0 ** n * 8  # f32 state bytes
     for k in (5, 6, 7):
         prog = zb.compile(p, k)
-        zb.run(p, shots=0, seed=1, precision=32, flags=zb.FLAG_TENSOR | zb.FLAG_FAST, program=prog)
-        t0 = time.perf_counter()
         r = zb.run(p, shots=0, seed=1, precision=32, flags=zb.FLAG_TENSOR | zb.FLAG_FAST, statevector=True,
                    program=prog)
-        t = time.perf_counter() - t0
         d = float(np.abs(r.statevector - ref.statevector).max())
         tvd = float(0.5 * np.abs(np.abs(r.statevector) ** 2 - np.abs(ref.statevector) ** 2).sum())
-        print(json.dumps({"workload": "%dq d60 gate mix, fused k=%d, f32 3xTF32" % (n, k), "seconds_incl_readback": t,
-                          "blocks": len(prog.ops), "max_fused": prog.stats["max_fused"],
-                          "max_abs_damp_vs_f64": d, "tvd_vs_f64": tvd}), flush=True)
+        be = zb.CudaBackend(n, 32, zb.FLAG_TENSOR | zb.FLAG_FAST)
+        _apply_ops(be, prog)
+        be.finish()
+        be.profile(True)
+        _apply_ops(be, prog)
+        be.finish()
+        prof = be.profile_read()
+        be.close()
+        blocks = [op for op in prog.ops if op.kind == zb.OP_UNITARY and len(op.qubits) >= 4]
+        flops = sum(8.0 * 2.0 ** (n + len(op.qubits)) for op in blocks)
+        kq = prof.get("tc_block", {"launches": 0, "ms": 0.0})
+        dev_ms = sum(v["ms"] for v in prof.values())
+        print(json.dumps({"workload": "%dq d60 gate mix, fused k=%d, f32 3xTF32" % (n, k),
+                          "device_ms": dev_ms, "tc_blocks": kq["launches"], "tc_ms": kq["ms"],
+                          "tc_ms_per_block": kq["ms"] / max(1, kq["launches"]),
+                          "tc_TFLOPs_algorithmic": flops / (kq["ms"] * 1e-3) / 1e12 if kq["ms"] else None,
+                          "tc_GBps": 2 * S * kq["launches"] / (kq["ms"] * 1e-3) / 1e9 if kq["ms"] else None,
+                          "kernels_ms": {k2: round(v["ms"], 3) for k2, v in prof.items()},
+                          "ops": len(prog.ops), "max_abs_damp_vs_f64": d, "tvd_vs_f64": tvd}), flush=True)
     prog1 = zb.compile(p, 1)
-    t0 = time.perf_counter()
+    be = zb.CudaBackend(n, 32, zb.FLAG_FAST)
+    _apply_ops(be, prog1)
+    be.finish()
+    be.profile(True)
+    _apply_ops(be, prog1)
+    be.finish()
+    prof = be.profile_read()
+    be.close()
     r = zb.run(p, shots=0, seed=1, precision=32, flags=zb.FLAG_FAST, statevector=True, program=prog1)
-    t = time.perf_counter() - t0
     d = float(np.abs(r.statevector - ref.statevector).max())
-    print(json.dumps({"workload": "%dq d60 gate mix, unfused sweeps f32 FMA" % n, "seconds_incl_readback": t,
+    print(json.dumps({"workload": "%dq d60 gate mix, unfused sweeps f32 FMA" % n,
+                      "device_ms": sum(v["ms"] for v in prof.values()),
+                      "kernels_ms": {k2: round(v["ms"], 3) for k2, v in prof.items()},
                       "ops": len(prog1.ops), "max_abs_damp_vs_f64": d}), flush=True)
 
 

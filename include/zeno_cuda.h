@@ -120,6 +120,11 @@ typedef struct {
 } zc_counters;
 int zc_get_counters(zc_state *st, zc_counters *out);
 
+/* Sweep tile shape: at most `max_high` (1..7) qubits above the 256-byte row
+ * per tile; 0 restores the automatic choice. Queued ops are flushed first.
+ * Used by the autotuner (zeno_gb300/autotune.py); results do not depend on it. */
+int zc_set_sweep_shape(zc_state *st, uint32_t max_high);
+
 /* Per-launch profiling: with profiling on, every kernel launch of this
  * state is bracketed by CUDA events on its stream. zc_profile(st, 1)
  * starts (and clears) a recording, zc_profile_read flushes, synchronises
@@ -215,6 +220,8 @@ typedef struct {
     uint64_t seed;
     const zc_noise *noise; /* NULL or trivial: ideal simulation */
     double mem_fraction;   /* budget fraction of device memory (0.75 when 0) */
+    uint32_t sweep_high;   /* sweep tile: high qubits per tile, 1..7 (0: automatic) */
+    uint32_t _pad;
 } zc_run_options;
 
 typedef struct {

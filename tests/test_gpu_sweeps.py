@@ -152,3 +152,21 @@ def test_fast_mode_qft_with_swaps(zc, oracle):
     dim = 1 << 16
     want = np.exp(2j * np.pi * x * np.arange(dim) / dim) / np.sqrt(dim)
     assert np.abs(r.statevector - want).max() < 1e-12
+
+
+def test_autotuned_runs_stay_bit_exact(zc, oracle):
+    """Exact mode: every (fusion, tile shape) the tuner may pick gives the
+    oracle's bits at that fusion; the tuner returns the fastest it timed."""
+    from zeno_gb300 import autotune as at
+
+    n = 16
+    p = C.matching_circuit(n, 6, 9).to_program()
+    for k, h in ((1, 4), (2, 7), (3, 5)):
+        prog = zc.compile(p, k)
+        r = zc.run(p, shots=0, precision=64, statevector=True, flags=zc.FLAG_EXACT | zc.FLAG_FORCE_SWEEPS,
+                   program=prog, sweep_high=h)
+        _, _, sv, _ = oracle.run(p, prec=64, shots=0, fusion=k, statevector=True)
+        assert np.array_equal(r.statevector.view(np.float64), sv.view(np.float64)), (k, h)
+    t = at.tune(p, 64, zc.FLAG_FAST, fusions=(1, 2), highs=(0, 5))
+    assert min(r["seconds"] for r in t["table"]) == [r["seconds"] for r in t["table"]
+                                                      if (r["fusion"], r["max_high"]) == (t["fusion"], t["max_high"])][0]

@@ -32,7 +32,7 @@ EXPORTS = (
     "zc_statevector", "zc_norm_sqr", "zc_finish", "zc_last_error", "zc_device_budget", "zc_state_bytes",
     "zc_max_qubits", "zc_load_state", "zc_get_stream", "zc_get_counters", "zc_compile", "zc_program_free",
     "zc_program_get_info", "zc_program_get_op", "zc_program_get_final", "zc_run", "zc_profile",
-    "zc_profile_read", "zc_sample_noalloc",
+    "zc_profile_read", "zc_sample_noalloc", "zc_set_sweep_shape",
 )
 
 
@@ -86,7 +86,8 @@ class NoiseC(C.Structure):
 
 class RunOptions(C.Structure):
     _fields_ = [("precision_bits", C.c_int), ("flags", C.c_uint32), ("shots", C.c_uint64), ("seed", C.c_uint64),
-                ("noise", C.POINTER(NoiseC)), ("mem_fraction", C.c_double)]
+                ("noise", C.POINTER(NoiseC)), ("mem_fraction", C.c_double), ("sweep_high", C.c_uint32),
+                ("_pad", C.c_uint32)]
 
 
 class RunResultC(C.Structure):
@@ -161,6 +162,7 @@ def load() -> C.CDLL:
         "zc_profile": ([vp, i32], i32),
         "zc_sample_noalloc": ([vp, u64, u64, P(u64)], i32),
         "zc_profile_read": ([vp, P(KernelStat), i32, P(i32)], i32),
+        "zc_set_sweep_shape": ([vp, u32], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -270,6 +272,10 @@ class CudaBackend:
     def profile(self, enable: bool = True) -> None:
         """Start (and clear) or stop per-launch CUDA-event recording."""
         _check(load().zc_profile(self._h, 1 if enable else 0))
+
+    def set_sweep_shape(self, max_high: int) -> None:
+        """At most `max_high` qubits above the row per sweep tile (0: automatic)."""
+        _check(load().zc_set_sweep_shape(self._h, max_high))
 
     def profile_read(self) -> Dict[str, Dict[str, float]]:
         """Per kernel class: launches, total ms, algorithmic bytes (flushes and syncs)."""
@@ -403,7 +409,7 @@ class RunResult:
 
 def run(p, shots: int = 1024, seed: int = 0, precision: int = 0, fusion: Optional[int] = None,
         noise: Optional[NoiseModel] = None, statevector: bool = False, flags: int = FLAG_EXACT,
-        program: Optional[Program] = None) -> RunResult:
+        program: Optional[Program] = None, sweep_high: int = 0) -> RunResult:
     """zeno::run_program with `--backend cuda` (src/lib.rs:224-250).
 
     Noisy runs compile with fusion 0 (src/lib.rs:228-231); the default dense
@@ -416,7 +422,7 @@ def run(p, shots: int = 1024, seed: int = 0, precision: int = 0, fusion: Optiona
     if program is None:
         program = compile(p, 0 if noisy else (1 if fusion is None else fusion))
     nz = NoiseC(*[getattr(noise, f.name) for f in fields(noise)]) if noisy else None
-    opts = RunOptions(precision, flags, shots, seed, C.pointer(nz) if nz is not None else None, 0.0)
+    opts = RunOptions(precision, flags, shots, seed, C.pointer(nz) if nz is not None else None, 0.0, sweep_high, 0)
     cap = max(16, min(shots, 1 << 22) + 1)
     keys = np.zeros(cap, dtype=np.uint64)
     counts = np.zeros(cap, dtype=np.uint64)

@@ -197,6 +197,7 @@ static SweepShape shape_for(const zc_state *st) {
     const uint32_t L = std::min<uint32_t>(st->n, st->prec == 64 ? 5 : 6);  // 256-byte rows
     const uint32_t Tmax = st->prec == 64 ? 12 : 13;                       // 64 KiB per tile buffer
     uint32_t Hcap = std::min<uint32_t>(Tmax - L, st->n - L);
+    if (st->sweep_high) return SweepShape{L, std::min<uint32_t>(Hcap, st->sweep_high)};  // tuned
     // keep at least ~2 tiles per SM so every SM streams
     uint32_t tiles_log2 = 0;
     while ((1u << tiles_log2) < (uint32_t)(2 * st->num_sms)) tiles_log2++;
@@ -773,6 +774,15 @@ int zc_profile_read(zc_state *st, zc_kernel_stat *out, int cap, int *n) {
         m++;
     }
     *n = m;
+    return ZC_OK;
+}
+
+int zc_set_sweep_shape(zc_state *st, uint32_t max_high) {
+    if (!st) return fail(ZC_ERR_INVALID, "null state");
+    if (max_high > kMaxSweepHigh) return fail(ZC_ERR_INVALID, "sweep shape: at most 7 high qubits per tile");
+    int rc = flush(st);  // queued ops keep the shape they were planned for
+    if (rc) return rc;
+    st->sweep_high = max_high;
     return ZC_OK;
 }
 

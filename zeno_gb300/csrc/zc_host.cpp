@@ -844,6 +844,10 @@ int zc_run(const zc_program *p, const zc_run_options *opt, zc_run_result *res, u
     zc_state *st = nullptr;
     rc = zc_create_ex(p->n_qubits, prec, opt->flags, &st);
     if (rc) return rc;
+    if (opt->sweep_high && (rc = zc_set_sweep_shape(st, opt->sweep_high))) {
+        zc_destroy(st);
+        return rc;
+    }
     std::vector<std::pair<uint64_t, uint64_t>> hist;
     auto done = [&](int code) {
         if (st) {

@@ -70,6 +70,7 @@ struct zc_state {
     uint32_t n = 0;
     int prec = 64;  // 32 or 64
     uint32_t flags = 0;
+    uint32_t sweep_high = 0;  // high (non-row) qubits per sweep tile; 0 = automatic
     int device = 0;
     int num_sms = 0;
     cudaStream_t stream = nullptr;

@@ -7,6 +7,7 @@
   python -m zeno_gb300.suite trajectories  # 4096 noisy 16q trajectories, batched vs per-shot
   python -m zeno_gb300.suite tc         # 28q gate mix fused to k=5..7 blocks on tensor cores vs FP64
   python -m zeno_gb300.suite sampler    # sample / prob_one per state size, exact and fast
+  python -m zeno_gb300.suite tune       # autotuner tables (fusion width x tile shape), 26 qubits
 
 Each prints JSON lines. Times are wall-clock around complete runs
 (`zc_run`: state allocation, ops, sampling), the semantics of zeno's
@@ -209,9 +210,24 @@ def sampler(args):
                 be.close()
 
 
+def tune(args):
+    """Autotuner tables: fusion width x tile shape, timed whole runs."""
+    from . import autotune as at
+
+    n = args.qubits
+    cases = [("%dq d40 u3+matching-CX f64 fast" % n, C.matching_circuit(n, 40, 7), 64, zb.FLAG_FAST),
+             ("%dq d40 u3+matching-CX f32 fast" % n, C.matching_circuit(n, 40, 7), 32, zb.FLAG_FAST),
+             ("%dq d60 gate mix f32 fast + tensor cores" % n, C.mixed_circuit(n, 60, 7), 32,
+              zb.FLAG_FAST | zb.FLAG_TENSOR)]
+    for name, c, prec, flags in cases:
+        t = at.tune(c, prec, flags)
+        print(json.dumps({"workload": name, "best_fusion": t["fusion"], "best_max_high": t["max_high"],
+                          "table": t["table"]}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["qft", "fusion", "big", "serving", "trajectories", "tc", "sampler"])
+    ap.add_argument("what", choices=["qft", "fusion", "big", "serving", "trajectories", "tc", "sampler", "tune"])
     ap.add_argument("--sizes", type=int, nargs="*", default=[16, 20, 22, 26, 28, 30])
     ap.add_argument("--qubits", type=int, default=None)
     ap.add_argument("--requests", type=int, default=1000)
@@ -220,7 +236,7 @@ def main():
     ap.add_argument("--server-only", action="store_true", help="serving: skip the one-circuit-per-call arm")
     a = ap.parse_args()
     if a.qubits is None:
-        a.qubits = {"fusion": 30, "big": 33, "tc": 28}.get(a.what, 30)
+        a.qubits = {"fusion": 30, "big": 33, "tc": 28, "tune": 26}.get(a.what, 30)
     zb.load()
     globals()[a.what](a)
 

@@ -239,14 +239,15 @@ typedef struct {
  * (exec::format_key, src/exec.rs:235-253). `statevector` (2^n c64) may be
  * NULL; it is rejected for dynamic or noisy programs.
  *
- * Noisy static programs at precision 32 run in the batched trajectory
- * engine (no counterpart in zeno, which replays shots one by one,
- * src/exec.rs:459-549): every shot is a trajectory with its own
- * Philox4x32-10 stream (key = seed, counter = (draw, shot)), all in one
- * launch; the channel order of src/noise.rs:145-175 is kept, results agree
- * with zeno's per-shot path in distribution. ZC_FLAG_PER_SHOT (or f64, or a
- * dynamic program) selects the per-shot replay, which reproduces zeno's RNG
- * stream layout. */
+ * Noisy or dynamic programs (mid-circuit measure, reset, conditioned ops)
+ * at precision 32 run in the batched trajectory engine (no counterpart in
+ * zeno, which replays shots one by one, src/exec.rs:459-619): every shot is
+ * a trajectory with its own Philox4x32-10 stream (key = seed, counter =
+ * (draw, shot)) and classical bits, all in one launch; the channel order of
+ * src/noise.rs:145-175 and the measure/reset/condition semantics of
+ * exec_shot_op are kept, results agree with zeno's per-shot path in
+ * distribution. ZC_FLAG_PER_SHOT (or f64) selects the per-shot replay,
+ * which reproduces zeno's RNG stream layout. */
 int zc_run(const zc_program *p, const zc_run_options *opt, zc_run_result *res, uint64_t *keys, uint64_t *counts,
            size_t cap, double *statevector);
 

@@ -16,10 +16,16 @@ pytestmark = pytest.mark.gpu
 
 
 def test_examples_match_oracle(zc, oracle, examples):
+    """Same counts as the oracle at the same seed. Dynamic programs take the
+    per-shot replay here (ZC_FLAG_PER_SHOT): at f32 they would otherwise run
+    as batched trajectories, which agree in distribution only
+    (tests/test_gpu_dynamic.py)."""
     for name, d in examples.items():
         p = program_from_json(d)
+        dynamic = zc.compile(p, 1).dynamic
         for prec in (64, 32):
-            mine = zc.run(p, shots=4000, seed=11, precision=prec, fusion=1)
+            flags = zc.FLAG_PER_SHOT if dynamic else zc.FLAG_EXACT
+            mine = zc.run(p, shots=4000, seed=11, precision=prec, fusion=1, flags=flags)
             ref, _, _, _ = oracle.run(p, prec=prec, shots=4000, seed=11, fusion=1)
             assert mine.counts == ref, (name, prec)
         exp = d["expected"]

@@ -647,29 +647,44 @@ void histogram(std::vector<uint64_t> &w, std::vector<std::pair<uint64_t, uint64_
 
 // Can the batched trajectory engine run this noisy program?
 bool batchable(const zc_program *p) {
-    if (p->dynamic) return false;
     for (const Op &o : p->ops) {
-        if (!o.gate_like()) return false;
+        const bool gate = o.kind == ZC_OP_UNITARY || o.kind == ZC_OP_DIAG || o.kind == ZC_OP_CX || o.kind == ZC_OP_SWAP;
+        if (!gate && o.kind != ZC_OP_MEASURE && o.kind != ZC_OP_RESET) return false;
         if ((o.kind == ZC_OP_UNITARY || o.kind == ZC_OP_DIAG) && o.qs.size() > 3) return false;
     }
-    return true;
+    return p->n_clbits <= 64;  // one classical word per trajectory, as the per-shot path
 }
 
-// Noisy static program, all shots as trajectories in one launch.
+// Noisy or dynamic program, all shots as trajectories in one launch.
 int run_batched(const zc_program *p, const zc_run_options *opt, const zc_noise &nz,
                 std::vector<std::pair<uint64_t, uint64_t>> *hist, zc_run_result *res) {
     std::vector<TrajOp> tops;
-    std::vector<double> mats;
+    std::vector<double> mats = {1, 0, 0, 0, 0, 0, 1, 0};  // 2x2 identity for measure / reset
     for (const Op &o : p->ops) {
-        std::vector<uint32_t> sup;
-        Mat m = dense_of(o, &sup);
         TrajOp t{};
-        t.k = (uint32_t)sup.size();
-        for (size_t i = 0; i < sup.size(); i++) t.qs[i] = sup[i];
-        t.mat_off = (uint32_t)mats.size();
-        for (const Cx &c : m) {
-            mats.push_back(c.re);
-            mats.push_back(c.im);
+        if (o.kind == ZC_OP_MEASURE || o.kind == ZC_OP_RESET) {
+            t.k = 1;
+            t.qs[0] = o.a;
+            t.kind = o.kind == ZC_OP_MEASURE ? TOP_MEASURE : TOP_RESET;
+            t.clbit = o.b;
+            t.mat_off = 0;
+        } else {
+            std::vector<uint32_t> sup;
+            Mat m = dense_of(o, &sup);
+            t.k = (uint32_t)sup.size();
+            for (size_t i = 0; i < sup.size(); i++) t.qs[i] = sup[i];
+            t.kind = TOP_GATE;
+            t.mat_off = (uint32_t)mats.size();
+            for (const Cx &c : m) {
+                mats.push_back(c.re);
+                mats.push_back(c.im);
+            }
+        }
+        if (o.has_if) {
+            t.cond = 1;
+            t.cond_off = o.creg_offset;
+            t.cond_len = o.creg_len;
+            t.cond_value = o.value;
         }
         tops.push_back(t);
     }
@@ -830,9 +845,10 @@ int zc_run(const zc_program *p, const zc_run_options *opt, zc_run_result *res, u
     if (prec == 0) prec = zc_state_bytes(p->n_qubits, 64) <= budget ? 64 : 32;
     res->precision_bits = prec;
     const auto t0 = std::chrono::steady_clock::now();
-    if (noise && prec == 32 && !(opt->flags & ZC_FLAG_PER_SHOT) && batchable(p)) {
+    if ((noise || p->dynamic) && prec == 32 && !(opt->flags & ZC_FLAG_PER_SHOT) && batchable(p)) {
         std::vector<std::pair<uint64_t, uint64_t>> hist;
-        rc = p->finals.empty() ? ZC_OK : run_batched(p, opt, *noise, &hist, res);
+        const zc_noise none{};
+        rc = p->finals.empty() && !p->dynamic ? ZC_OK : run_batched(p, opt, noise ? *noise : none, &hist, res);
         res->sim_seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         res->n_keys = hist.size();
         for (size_t i = 0; i < hist.size() && i < cap; i++) {

@@ -105,6 +105,8 @@ struct Shared {
     double seg[kTrajThreads];
     uint64_t draw;                // next draw number of this trajectory
     uint64_t pick;                // sampled basis index
+    uint64_t cl;                  // classical bits of this trajectory
+    int skip;                     // the current op's condition is false
     int fail;
 };
 
@@ -211,15 +213,26 @@ __global__ void __launch_bounds__(kTrajThreads)
         if (tid == 0) {
             s.npend = 0;
             s.draw = 0;
+            s.cl = 0;
         }
         __syncthreads();
         for (int o = 0; o < nops; o++) {
             const TrajOp op = ops[o];
             const uint32_t k = op.k, dim = 1u << k;
-            // ---- thread 0: depolarizing draws, gate x Pauli string, pending factors
+            const bool gate = op.kind == TOP_GATE;
+            // ---- thread 0: condition, depolarizing draws, gate x Pauli string, pending factors
+            if (tid == 0) {
+                s.skip = 0;
+                if (op.cond) {
+                    const uint64_t mask = op.cond_len >= 64 ? ~0ull : ((1ull << op.cond_len) - 1);
+                    s.skip = ((s.cl >> op.cond_off) & mask) != op.cond_value;
+                }
+            }
+            __syncthreads();
+            if (s.skip) continue;  // pending operators wait for the next op that runs
             if (tid == 0) {
                 prepare_pending(s);
-                const double pdep = k == 1 ? nz.p[0] : nz.p[1];
+                const double pdep = gate ? (k == 1 ? nz.p[0] : nz.p[1]) : 0.0;
                 uint64_t idx = 0;
                 if (pdep > 0.0 && philox_f64(seed, t, s.draw++) < pdep)
                     idx = 1 + philox_range(seed, t, s.draw++, (1ull << (2 * k)) - 1);
@@ -277,8 +290,27 @@ __global__ void __launch_bounds__(kTrajThreads)
             __syncthreads();
             if (tid == 0) s.npend = 0;
             reduce_table(s, hi, lo, (int)dim);
+            // ---- thread 0, measure / reset: outcome from the table, collapse (and X) left pending
+            if (tid == 0 && !gate) {
+                const double tot = s.J[0] + s.J[1];
+                const double p1 = tot > 0.0 ? s.J[1] / tot : 0.0;
+                const bool one = philox_f64(seed, t, s.draw++) < p1;  // src/exec.rs:201-207
+                const double sc = 1.0 / sqrt(one ? p1 : 1.0 - p1);
+                Pending &P = s.pend[s.npend++];
+                P.q = op.qs[0];
+                for (int i = 0; i < 4; i++) P.m[i] = C2{0, 0};
+                if (!one) P.m[0] = C2{sc, 0};
+                else if (op.kind == TOP_RESET) P.m[1] = C2{sc, 0};  // X . diag(0, sc)
+                else P.m[3] = C2{sc, 0};
+                if (op.kind == TOP_MEASURE) {
+                    bool bit = one;
+                    const double pr = bit ? nz.p[6] : nz.p[5];  // readout_flip (src/noise.rs:181-192)
+                    if (pr > 0.0 && philox_f64(seed, t, s.draw++) < pr) bit = !bit;
+                    s.cl = (s.cl & ~(1ull << op.clbit)) | ((uint64_t)bit << op.clbit);
+                }
+            }
             // ---- thread 0: flips and damping on the table, in the reference's order
-            if (tid == 0) {
+            if (tid == 0 && gate) {
                 double J[8];
                 for (uint32_t j = 0; j < dim; j++) J[j] = s.J[j];
                 for (uint32_t b = 0; b < k; b++) {
@@ -391,7 +423,7 @@ __global__ void __launch_bounds__(kTrajThreads)
                     }
                 }
             }
-            uint64_t cl = 0;
+            uint64_t cl = s.cl;
             for (int f = 0; f < nfinal; f++) {
                 bool bit = (pick >> fq[f]) & 1;
                 const double pr = bit ? nz.p[6] : nz.p[5];

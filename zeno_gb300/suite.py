@@ -8,6 +8,7 @@
   python -m zeno_gb300.suite tc         # 28q gate mix fused to k=5..7 blocks on tensor cores vs FP64
   python -m zeno_gb300.suite sampler    # sample / prob_one per state size, exact and fast
   python -m zeno_gb300.suite tune       # autotuner tables (fusion width x tile shape), 26 qubits
+  python -m zeno_gb300.suite dynamic    # 16q dynamic circuit, 4096 shots: batched trajectories vs per-shot
 
 Each prints JSON lines. Times are wall-clock around complete runs
 (`zc_run`: state allocation, ops, sampling), the semantics of zeno's
@@ -210,6 +211,43 @@ def sampler(args):
                 be.close()
 
 
+def dynamic(args):
+    """Dynamic circuit (mid-circuit measure + conditional gate + reset after
+    every layer): all shots as batched trajectories vs zeno's per-shot replay."""
+    import math
+
+    import numpy as np
+
+    n, layers, shots = args.qubits, 6, 4096
+    rng = np.random.default_rng(21)
+    cregs = [("m%d" % i, 1) for i in range(layers)] + [("f", n)]
+    p = C.Program(n, cregs, [])
+    for layer in range(layers):
+        for q in range(n):
+            p.instrs.append(C.Instr(C.I_GATE, "u3", (q,), tuple(float(x) for x in rng.uniform(0, 2 * math.pi, 3))))
+        for q in range(layer % 2, n - 1, 2):
+            p.instrs.append(C.Instr(C.I_GATE, "cx", (q, q + 1)))
+        mq = int(rng.integers(n))
+        p.instrs.append(C.Instr(C.I_MEASURE, qubits=(mq,), clbit=layer))
+        p.instrs.append(C.Instr(C.I_GATE, "x", ((mq + 1) % n,), (), 0, layer, 1))
+        p.instrs.append(C.Instr(C.I_RESET, qubits=(mq,)))
+    for q in range(n):
+        p.instrs.append(C.Instr(C.I_MEASURE, qubits=(q,), clbit=layers + q))
+    prog = zb.compile(p, 0)
+    zb.run(p, shots=64, seed=1, precision=32, program=prog)
+    t0 = time.perf_counter()
+    r = zb.run(p, shots=shots, seed=2, precision=32, program=prog)
+    tb = time.perf_counter() - t0
+    per = 32
+    t0 = time.perf_counter()
+    zb.run(p, shots=per, seed=2, precision=32, program=prog, flags=zb.FLAG_PER_SHOT)
+    tp = (time.perf_counter() - t0) / per
+    print(json.dumps({"workload": "%dq %d-layer dynamic circuit (measure + if + reset per layer), %d shots"
+                      % (n, layers, shots), "batched": r.batched, "batched_seconds": tb,
+                      "shots_per_s": shots / tb, "per_shot_shots_per_s": 1 / tp, "speedup": tp * shots / tb,
+                      "launches": r.launches, "keys": len(r.counts)}), flush=True)
+
+
 def tune(args):
     """Autotuner tables: fusion width x tile shape, timed whole runs."""
     from . import autotune as at
@@ -227,7 +265,8 @@ def tune(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["qft", "fusion", "big", "serving", "trajectories", "tc", "sampler", "tune"])
+    ap.add_argument("what", choices=["qft", "fusion", "big", "serving", "trajectories", "tc", "sampler", "tune",
+                                       "dynamic"])
     ap.add_argument("--sizes", type=int, nargs="*", default=[16, 20, 22, 26, 28, 30])
     ap.add_argument("--qubits", type=int, default=None)
     ap.add_argument("--requests", type=int, default=1000)
@@ -236,7 +275,7 @@ def main():
     ap.add_argument("--server-only", action="store_true", help="serving: skip the one-circuit-per-call arm")
     a = ap.parse_args()
     if a.qubits is None:
-        a.qubits = {"fusion": 30, "big": 33, "tc": 28, "tune": 26}.get(a.what, 30)
+        a.qubits = {"fusion": 30, "big": 33, "tc": 28, "tune": 26, "dynamic": 16}.get(a.what, 30)
     zb.load()
     globals()[a.what](a)
 

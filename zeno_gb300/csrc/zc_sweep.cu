@@ -248,7 +248,8 @@ struct SweepSmem {
     uint64_t bar;
     MicroOp ops[kMaxMicroOps];
     OpCoef<T, A> coef[kMaxMicroOps];
-    uint32_t hpos[16];
+    uint32_t hpos[16];     // tile bit L + j holds qubit hpos[j] (any order)
+    uint32_t hsorted[16];  // the same qubits ascending (tile base)
     uint64_t row_off[1 << kMaxSweepHigh];
     int nops;
     uint32_t L, H;
@@ -266,6 +267,13 @@ __device__ void load_job(SweepSmem<T, A> &c, const MicroOp *gops, int nops, uint
     for (int i = tid; i < nops * (int)(sizeof(MicroOp) / 4); i += blockDim.x)
         reinterpret_cast<uint32_t *>(c.ops)[i] = reinterpret_cast<const uint32_t *>(gops)[i];
     if (tid < 16) c.hpos[tid] = tid < (int)H ? hpos[tid] : 0u;
+    if (tid == 0) {
+        for (uint32_t j = 0; j < H; j++) {  // insertion sort, H <= 7
+            uint32_t x = hpos[j], i = j;
+            for (; i > 0 && c.hsorted[i - 1] > x; i--) c.hsorted[i] = c.hsorted[i - 1];
+            c.hsorted[i] = x;
+        }
+    }
     for (uint32_t r = tid; r < (1u << H); r += blockDim.x) {
         uint64_t o = 0;
         for (uint32_t j = 0; j < H; j++) o |= (uint64_t)((r >> j) & 1) << hpos[j];
@@ -305,7 +313,7 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
     const uint32_t size = 1u << (c.L + c.H);
     const uint32_t rows = 1u << c.H, row_elems = 1u << c.L, row_bytes = row_elems * (uint32_t)sizeof(T);
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
-    const uint64_t base = tile_base(t, c.L, c.hpos, c.H);
+    const uint64_t base = tile_base(t, c.L, c.hsorted, c.H);
     if (warp == 0) {
         if (lane == 0) mbar_expect_tx(&c.bar, 2u * rows * row_bytes);
         __syncwarp();

@@ -25,6 +25,7 @@ namespace {
 
 constexpr int kSweepThreads = 256;
 constexpr int kSweepCtasPerSm = 3;
+constexpr uint32_t kJlutHigh = 1u << (13 - 8);  // tile index values above the low byte (tiles <= 2^13)
 // Global index of the first element of tile t: the tile number fills the
 // non-local positions above the L low bits.
 __device__ __forceinline__ uint64_t tile_base(uint64_t t, uint32_t L, const uint32_t *hpos, uint32_t H) {
@@ -167,7 +168,7 @@ __device__ void apply_u1_group(R *sr, R *si, const MicroOp *ops, const OpCoef<T,
 // slots hold (hi, lo) float pairs (R = float2); otherwise R = T.
 template <typename T, int A, typename R>
 __device__ void apply_ops(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *coef, int nops, uint64_t base,
-                          uint32_t size, const char *tables, uint32_t *bad) {
+                          uint32_t size, const char *tables, uint32_t *bad, uint16_t *jlut) {
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int o = 0; o < nops; o++) {
         const MicroOp &op = ops[o];
@@ -227,8 +228,13 @@ __device__ void apply_ops(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *
             const uint32_t jo = jouter(op, base);
             const T *dre = reinterpret_cast<const T *>(tables + op.table);
             const T *dim_ = dre + (1u << op.k);
+            // table index of element v = jo | lut[v & 255] | lut[256 + (v >> 8)]:
+            // the op's local bits gathered once per op instead of per element
+            for (uint32_t x = tid; x < 256 + kJlutHigh; x += nt)
+                jlut[x] = (uint16_t)jgather<R>(op, 0u, x < 256 ? x : (x - 256) << 8);
+            __syncthreads();
             for (uint32_t v = tid; v < size; v += nt) {
-                const uint32_t j = jgather<R>(op, jo, v);
+                const uint32_t j = jo | jlut[v & 255u] | jlut[256 + (v >> 8)];
                 if constexpr (A == AR_DF)
                     cscale_df(df_from_f64(__ldg(dre + j)), df_from_f64(__ldg(dim_ + j)), sr[v], si[v]);
                 else
@@ -256,6 +262,7 @@ struct SweepSmem {
     int has_arith;
     int fail;
     uint32_t fail_tile, done_tiles, bad;
+    uint16_t jlut[256 + kJlutHigh];  // diagonal index tables of the current DK op
 };
 
 // All threads: make (gops, nops, L, H, hpos) the CTA's current job.
@@ -341,7 +348,7 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
             }
             __syncthreads();
         }
-        apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables, &c.bad);
+        apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut);
         if (c.has_arith) {
             for (uint32_t v = tid; v < size; v += blockDim.x) {
                 dr[v] = df_to_f64(fr[v]);
@@ -349,7 +356,7 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
             }
         }
     } else {
-        apply_ops<T, A, T>(sre, sim, c.ops, c.coef, c.nops, base, size, tables, &c.bad);
+        apply_ops<T, A, T>(sre, sim, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut);
     }
     fence_async_smem();
     __syncthreads();

@@ -197,33 +197,41 @@ __device__ void apply_ops(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *
                 continue;
             }
             const uint32_t b = op.a;
-            if constexpr (A == AR_DF) {
-                MatDF m;
+            typename std::conditional<A == AR_DF, MatDF, Mat2<T>>::type m;
 #pragma unroll
-                for (int i = 0; i < 8; i++) m.v[i] = coef[o].v[i];
-                for (uint32_t p = tid; p < size / 2; p += nt) {
-                    const uint32_t v0 = ((p >> b) << (b + 1)) | (p & ((1u << b) - 1)), v1 = v0 | (1u << b);
-                    pair_update_df(m, sr[v0], si[v0], sr[v1], si[v1]);
-                }
-            } else {
-                Mat2<T> m;
-#pragma unroll
-                for (int i = 0; i < 8; i++) m.v[i] = coef[o].v[i];
-                for (uint32_t p = tid; p < size / 2; p += nt) {
-                    const uint32_t v0 = ((p >> b) << (b + 1)) | (p & ((1u << b) - 1)), v1 = v0 | (1u << b);
-                    pair_update<T, A == AR_EXACT>(m, sr[v0], si[v0], sr[v1], si[v1]);
-                }
+            for (int i = 0; i < 8; i++) m.v[i] = coef[o].v[i];
+            auto upd = [&](R &ar, R &ai, R &br, R &bi) {
+                if constexpr (A == AR_DF) pair_update_df(m, ar, ai, br, bi);
+                else pair_update<T, A == AR_EXACT>(m, ar, ai, br, bi);
+            };
+            for (uint32_t p = tid; p < size / 2; p += nt) {
+                const uint32_t v0 = ((p >> b) << (b + 1)) | (p & ((1u << b) - 1)), v1 = v0 | (1u << b);
+                upd(sr[v0], si[v0], sr[v1], si[v1]);
             }
         } else if (op.kind == MOP_D1) {
             const bool outer = op.a & kOuterFlag;
             const bool tile_one = outer && ((base >> (op.a & ~kOuterFlag)) & 1);
-            for (uint32_t v = tid; v < size; v += nt) {
+            auto scl = [&](uint32_t v, R &xr, R &xi) {
                 const bool one = outer ? tile_one : ((v >> op.a) & 1);
-                if constexpr (A == AR_DF)
-                    cscale_df(coef[o].v[one ? 2 : 0], coef[o].v[one ? 3 : 1], sr[v], si[v]);
-                else
-                    cscale<T, A == AR_EXACT>(coef[o].v[one ? 2 : 0], coef[o].v[one ? 3 : 1], sr[v], si[v]);
+                if constexpr (A == AR_DF) cscale_df(coef[o].v[one ? 2 : 0], coef[o].v[one ? 3 : 1], xr, xi);
+                else cscale<T, A == AR_EXACT>(coef[o].v[one ? 2 : 0], coef[o].v[one ? 3 : 1], xr, xi);
+            };
+            uint32_t v = tid;
+            for (; v + 3u * nt < size; v += 4u * nt) {
+                R xr[4], xi[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    xr[k] = sr[v + k * nt];
+                    xi[k] = si[v + k * nt];
+                }
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    scl(v + k * nt, xr[k], xi[k]);
+                    sr[v + k * nt] = xr[k];
+                    si[v + k * nt] = xi[k];
+                }
             }
+            for (; v < size; v += nt) scl(v, sr[v], si[v]);
         } else if (op.kind == MOP_DK) {
             const uint32_t jo = jouter(op, base);
             const T *dre = reinterpret_cast<const T *>(tables + op.table);
@@ -233,12 +241,33 @@ __device__ void apply_ops(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *
             for (uint32_t x = tid; x < 256 + kJlutHigh; x += nt)
                 jlut[x] = (uint16_t)jgather<R>(op, 0u, x < 256 ? x : (x - 256) << 8);
             __syncthreads();
-            for (uint32_t v = tid; v < size; v += nt) {
+            auto scl = [&](T wr, T wi, R &xr, R &xi) {
+                if constexpr (A == AR_DF) cscale_df(df_from_f64(wr), df_from_f64(wi), xr, xi);
+                else cscale<T, A == AR_EXACT>(wr, wi, xr, xi);
+            };
+            uint32_t v = tid;
+            for (; v + 3u * nt < size; v += 4u * nt) {
+                R xr[4], xi[4];
+                T wr[4], wi[4];
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const uint32_t vk = v + k * nt;
+                    const uint32_t j = jo | jlut[vk & 255u] | jlut[256 + (vk >> 8)];
+                    wr[k] = __ldg(dre + j);
+                    wi[k] = __ldg(dim_ + j);
+                    xr[k] = sr[vk];
+                    xi[k] = si[vk];
+                }
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    scl(wr[k], wi[k], xr[k], xi[k]);
+                    sr[v + k * nt] = xr[k];
+                    si[v + k * nt] = xi[k];
+                }
+            }
+            for (; v < size; v += nt) {
                 const uint32_t j = jo | jlut[v & 255u] | jlut[256 + (v >> 8)];
-                if constexpr (A == AR_DF)
-                    cscale_df(df_from_f64(__ldg(dre + j)), df_from_f64(__ldg(dim_ + j)), sr[v], si[v]);
-                else
-                    cscale<T, A == AR_EXACT>(__ldg(dre + j), __ldg(dim_ + j), sr[v], si[v]);
+                scl(__ldg(dre + j), __ldg(dim_ + j), sr[v], si[v]);
             }
         } else {
             apply_perm(sr, si, op, base, size);

@@ -1,12 +1,14 @@
 """Kernel micro-benchmarks for the GB300 backend (CUDA-event timing).
 
   python -m zeno_gb300.microbench [--qubits 28 30] [--fp-peaks]
+  python -m zeno_gb300.microbench --sweep-costs 26
 
 Per state size, precision and arithmetic mode: one-qubit gate passes on
 low and high qubits, CX, a 3-qubit diagonal, dense k-qubit blocks, a sweep
 of 1/4/7 one-qubit gates, sampling and prob_one; each reported as time and
 algorithmic GB/s (2S per pass, S for CX). `--fp-peaks` compiles and runs
-probes/fp_peaks.cu (FP64 and FP32 instruction rates).
+probes/fp_peaks.cu (FP64 and FP32 instruction rates). `--sweep-costs N`
+prints the cost of one micro-op of each kind inside a sweep.
 """
 
 import argparse
@@ -38,6 +40,21 @@ def timed(be, torch, fn, reps=3):
     for _ in range(reps):
         fn()
     be.finish()
+    e1.record(s)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def timed_flush(be, torch, fn, reps=3):
+    """Device time per call of fn followed by a flush (one sweep per call)."""
+    s = torch.cuda.ExternalStream(be.stream())
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    fn()
+    be.finish()
+    e0.record(s)
+    for _ in range(reps):
+        fn()
+        be.finish()
     e1.record(s)
     torch.cuda.synchronize()
     return e0.elapsed_time(e1) / reps
@@ -82,15 +99,56 @@ def kernels(qubits):
                 be.close()
 
 
+def sweep_costs(n):
+    """Cost of one micro-op of each kind inside a sweep: a flush of 1 and of
+    32 ops of that kind (one sweep each, same tile), per-op time = the
+    difference / 31, per amplitude in ns and in SM cycles at 2.07 GHz."""
+    import torch
+
+    from . import backend as zc
+
+    zc.load()
+    rng = np.random.default_rng(1)
+
+    def unitary(d):
+        return np.linalg.qr(rng.normal(size=(d, d)) + 1j * rng.normal(size=(d, d)))[0]
+
+    kinds = {
+        "u1 q=1 (row bit)": lambda be, i: be.apply_unitary([1], unitary(2)),
+        "u1 q=n-1 (high bit)": lambda be, i: be.apply_unitary([n - 1], unitary(2)),
+        "u1 alternating q=0,n-1,n-2": lambda be, i: be.apply_unitary([(0, n - 1, n - 2)[i % 3]], unitary(2)),
+        "cx 2->n-1": lambda be, i: be.apply_cx(2, n - 1),
+        "swap 1<->n-2": lambda be, i: be.apply_swap(1, n - 2),
+        "diag1 q=n-1": lambda be, i: be.apply_diagonal([n - 1], np.exp(1j * rng.uniform(0, 6.3, 2))),
+        "diag4": lambda be, i: be.apply_diagonal([0, 3, n - 2, n - 1], np.exp(1j * rng.uniform(0, 6.3, 16))),
+        "diag10": lambda be, i: be.apply_diagonal(list(range(0, 20, 2)), np.exp(1j * rng.uniform(0, 6.3, 1024))),
+    }
+    for prec, flags, mode in ((32, zc.FLAG_FAST, "fma"), (32, zc.FLAG_EXACT, "exact"), (64, zc.FLAG_FAST, "df"),
+                              (64, zc.FLAG_EXACT, "exact")):
+        be = zc.CudaBackend(n, prec, flags)
+        for name, f in kinds.items():
+            t1 = timed_flush(be, torch, lambda: f(be, 0))
+            t32 = timed_flush(be, torch, lambda: [f(be, i) for i in range(32)])
+            per = (t32 - t1) / 31
+            ns_amp = per * 1e6 / (1 << n)
+            print("n=%d f%d %-5s %-28s sweep(1) %8.3f ms  sweep(32) %8.3f ms  per op %7.3f ms  %6.3f ns/amp  "
+                  "%6.1f SM-cycles/amp/SM" % (n, prec, mode, name, t1, t32, per, ns_amp, ns_amp * 2.07 * 152),
+                  flush=True)
+        be.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--qubits", type=int, nargs="*", default=[28, 30])
     ap.add_argument("--fp-peaks", action="store_true")
+    ap.add_argument("--sweep-costs", type=int, default=0, metavar="N", help="per-micro-op costs at N qubits")
     a = ap.parse_args()
     sys.path.insert(0, os.path.dirname(HERE))
     if a.fp_peaks:
         fp_peaks()
-    if a.qubits:
+    if a.sweep_costs:
+        sweep_costs(a.sweep_costs)
+    elif a.qubits:
         kernels(a.qubits)
 
 

@@ -100,6 +100,15 @@ const char *zc_last_error(void);
 /* Device memory a state may use: ZENO_MEM_BYTES if set (mem.rs:11-16),
  * else `fraction` of the device's total HBM. */
 int zc_device_budget(double fraction, uint64_t *bytes);
+
+/* The current device, for capacity reports (zeno info, src/main.rs:1001-1082
+ * with HBM in place of RAM). */
+typedef struct {
+    char name[64];
+    uint32_t sms, cc_major, cc_minor, _pad;
+    uint64_t hbm_bytes, free_bytes, l2_bytes;
+} zc_device;
+int zc_device_info(zc_device *out);
 uint64_t zc_state_bytes(uint32_t n_qubits, int precision_bits);
 uint32_t zc_max_qubits(uint64_t budget, int precision_bits);
 

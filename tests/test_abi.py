@@ -65,3 +65,15 @@ def test_invalid_arguments_rejected_before_device(zc, monkeypatch):
     monkeypatch.setenv("ZENO_MEM_BYTES", str(1 << 20))
     with pytest.raises(zc.ZenoCudaError):
         zc.CudaBackend(4, 48)  # bad precision
+
+
+def test_info_capacity_rows(zc, monkeypatch):
+    """The info table's rows come from the same capacity math (no device needed
+    for the rows themselves)."""
+    from zeno_gb300 import info
+
+    budget = int(284208 * (1 << 20) * 0.75)
+    f64, f32 = info.capacity(budget, 64), info.capacity(budget, 32)
+    assert (f64["max_qubits"], f32["max_qubits"]) == (33, 34)
+    assert f64["state_bytes"] == 128 << 30 and f64["next_qubit_bytes"] == 256 << 30
+    assert info.human(128 << 30) == "128.0 GiB" and info.human(512) == "512 B"

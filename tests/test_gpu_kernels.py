@@ -191,3 +191,13 @@ def test_capacity_refusal(zc):
     with pytest.raises(zc.ZenoCudaError) as e:
         zc.CudaBackend(40, 64)
     assert e.value.code == zc.ZC_ERR_MEMORY and "max 33 qubits" in str(e.value)
+
+
+def test_device_info_report(zc):
+    from zeno_gb300 import info
+
+    r = info.report()
+    assert r["sms"] >= 100 and r["hbm_bytes"] > 100e9 and r["l2_bytes"] > 50e6
+    assert r["budget_bytes"] == int(r["hbm_bytes"] * 0.75) or "ZENO_MEM_BYTES" in __import__("os").environ
+    f64 = r["precisions"]["f64"]
+    assert f64["state_bytes"] <= r["budget_bytes"] < f64["next_qubit_bytes"]

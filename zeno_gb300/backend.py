@@ -32,8 +32,14 @@ EXPORTS = (
     "zc_statevector", "zc_norm_sqr", "zc_finish", "zc_last_error", "zc_device_budget", "zc_state_bytes",
     "zc_max_qubits", "zc_load_state", "zc_get_stream", "zc_get_counters", "zc_compile", "zc_program_free",
     "zc_program_get_info", "zc_program_get_op", "zc_program_get_final", "zc_run", "zc_profile",
-    "zc_profile_read", "zc_sample_noalloc", "zc_set_sweep_shape",
+    "zc_profile_read", "zc_sample_noalloc", "zc_set_sweep_shape", "zc_device_info",
 )
+
+
+class DeviceC(C.Structure):
+    _fields_ = [("name", C.c_char * 64), ("sms", C.c_uint32), ("cc_major", C.c_uint32), ("cc_minor", C.c_uint32),
+                ("_pad", C.c_uint32), ("hbm_bytes", C.c_uint64), ("free_bytes", C.c_uint64),
+                ("l2_bytes", C.c_uint64)]
 
 
 class ZenoCudaError(RuntimeError):
@@ -163,6 +169,7 @@ def load() -> C.CDLL:
         "zc_sample_noalloc": ([vp, u64, u64, P(u64)], i32),
         "zc_profile_read": ([vp, P(KernelStat), i32, P(i32)], i32),
         "zc_set_sweep_shape": ([vp, u32], i32),
+        "zc_device_info": ([P(DeviceC)], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -439,6 +446,13 @@ def run(p, shots: int = 1024, seed: int = 0, precision: int = 0, fusion: Optiona
     prec = res.precision_bits
     return RunResult(fmt, raw, shots, p.n_qubits, prec, "cuda-f%d" % prec, seed, res.sim_seconds, sv,
                      program.stats, res.launches, res.sweeps, res.bytes_moved, bool(res.batched))
+
+
+def device_info() -> Dict[str, object]:
+    d = DeviceC()
+    _check(load().zc_device_info(C.byref(d)))
+    return {"name": d.name.decode(), "sms": d.sms, "compute_capability": "%d.%d" % (d.cc_major, d.cc_minor),
+            "hbm_bytes": d.hbm_bytes, "free_bytes": d.free_bytes, "l2_bytes": d.l2_bytes}
 
 
 def device_budget(fraction: float = 0.75) -> int:

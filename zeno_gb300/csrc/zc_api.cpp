@@ -491,6 +491,25 @@ int zc_device_budget(double fraction, uint64_t *bytes) {
     return ZC_OK;
 }
 
+int zc_device_info(zc_device *out) {
+    if (!out) return fail(ZC_ERR_INVALID, "null output");
+    memset(out, 0, sizeof *out);
+    int dev = 0;
+    ZC_CUDA(cudaGetDevice(&dev));
+    cudaDeviceProp prop;
+    ZC_CUDA(cudaGetDeviceProperties(&prop, dev));
+    snprintf(out->name, sizeof out->name, "%s", prop.name);
+    out->sms = (uint32_t)prop.multiProcessorCount;
+    out->cc_major = (uint32_t)prop.major;
+    out->cc_minor = (uint32_t)prop.minor;
+    size_t free_b = 0, total_b = 0;
+    ZC_CUDA(cudaMemGetInfo(&free_b, &total_b));
+    out->hbm_bytes = total_b;
+    out->free_bytes = free_b;
+    out->l2_bytes = (uint64_t)prop.l2CacheSize;
+    return ZC_OK;
+}
+
 int zc_create(uint32_t n, int prec, zc_state **out) { return zc_create_ex(n, prec, ZC_FLAG_EXACT, out); }
 
 int zc_create_ex(uint32_t n, int prec, uint32_t flags, zc_state **out) {

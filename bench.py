@@ -38,6 +38,11 @@ HBM_FALLBACK_GBS = 6800.0
 MEASURED_TRAFFIC_RATIO = {"sweep": (1.075e9 + 1.023e9) / 2.147e9}
 # The same capture: issue slots 73% busy, FMA pipe 58%, FP64 pipe 0%.
 SWEEP_DF_PIPES = {"issue_active_pct": 73.0, "fma_pipe_pct": 58.0, "fp64_pipe_pct": 0.0}
+# Double-float arithmetic of one 2x2 gate: four dot products of four products
+# (df_dot4: 4 x 4 FP32 instructions for the products, 3 TwoSums of 6, 7 adds,
+# 3 to renormalise = 44 per output component) = 176 per amplitude pair.
+DF_FP32_INSTR_PER_AMP_1Q = 88
+FP32_INSTR_PEAK = 34.3e12  # measured FMA issue rate (zeno_gb300/probes/fp_peaks.cu)
 
 
 def parse():
@@ -336,6 +341,7 @@ def main():
     be.profile(False)
     value, elapsed = job_throughput(a.steps, elapsed, ws)
     gates_ms = sum(d["ms"] for d in classes.values())  # all of our kernels in the timed region
+    n1q = sum(1 for op in ops if op.kind == zc.OP_UNITARY and len(op.qubits) == 1)
     dom = max(classes, key=lambda c: classes[c]["ms"])
     dd = classes[dom]
     peak, peak_kind = peaks()
@@ -363,6 +369,15 @@ def main():
                      "ops_per_launch": len(ops) * a.steps / dd["launches"] if dom == "sweep" else 1.0,
                      "limiter": ("FP32/ALU issue: each sweep applies many gates per HBM pass in double-float "
                                  "arithmetic; ncu at 26q: %s" % SWEEP_DF_PIPES)
+                     if dom == "sweep" and a.mode == "fast" and a.precision == 64 else None,
+                     "compute": ({"bound": "fp32_pipe", "unit": "FP32 instr/s",
+                                  "achieved": n1q * a.steps * DF_FP32_INSTR_PER_AMP_1Q * (1 << a.qubits) / (dd["ms"] / 1e3),
+                                  "peak": FP32_INSTR_PEAK,
+                                  "frac": n1q * a.steps * DF_FP32_INSTR_PER_AMP_1Q * (1 << a.qubits) / (dd["ms"] / 1e3)
+                                  / FP32_INSTR_PEAK,
+                                  "count": "one-qubit gates x 88 FP32 instructions per amplitude (double-float "
+                                           "2x2 update); CX/SWAP moves and f64 <-> double-float conversions not "
+                                           "counted"})
                      if dom == "sweep" and a.mode == "fast" and a.precision == 64 else None},
         "clocks": clk.summary(),
     }

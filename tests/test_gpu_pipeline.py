@@ -82,10 +82,12 @@ def test_mixed_circuit_f32_vs_f64(zc):
     assert np.abs(a - b).max() < 2e-4
 
 
-@pytest.mark.parametrize("n,prec", [(26, 64), (28, 32)])
-def test_full_size_inverse_round_trip(zc, n, prec):
-    """U followed by U^dagger returns |0...0> (size-independent property)."""
-    c = C.matching_circuit(n, 3, 99, measure=False)
+@pytest.mark.parametrize("n,prec,depth,fast", [(26, 64, 3, False), (28, 32, 3, False), (30, 64, 40, True)])
+def test_full_size_inverse_round_trip(zc, n, prec, depth, fast):
+    """U followed by U^dagger returns |0...0> (size-independent property);
+    the last case is the headline workload itself (30 qubits, depth 40, f64,
+    double-float arithmetic)."""
+    c = C.matching_circuit(n, depth, 99, measure=False)
     inv = C.Circuit(n)
     for ins in reversed(c.instrs):
         if ins.name == "u3":
@@ -93,7 +95,7 @@ def test_full_size_inverse_round_trip(zc, n, prec):
             inv.u(ins.qubits[0], -t, -la, -ph)
         else:
             inv.gate(ins.name, ins.qubits, ins.params)
-    g = zc.CudaBackend(n, prec)
+    g = zc.CudaBackend(n, prec, zc.FLAG_FAST if fast else zc.FLAG_EXACT)
     for prog in (c, inv):
         for op in zc.compile(prog.to_program(), 1).ops:
             if op.kind == zc.OP_UNITARY:
@@ -101,7 +103,10 @@ def test_full_size_inverse_round_trip(zc, n, prec):
             elif op.kind == zc.OP_CX:
                 g.apply_cx(op.a, op.b)
     tol = 1e-12 if prec == 64 else 1e-5
-    assert abs(g.norm_sqr() - 1) < tol * 10
+    # double-float: the f64 <-> (hi, lo) conversions truncate, so the norm
+    # drifts down by ~6e-15 per gate; 3600 gates at 30 qubits stay below 1e-10
+    norm_tol = 1e-10 if fast else tol * 10
+    assert abs(g.norm_sqr() - 1) < norm_tol
     assert abs(g.prob_one(n - 1)) < tol
     s = g.sample(1000, 1)
     assert np.all(s == 0)

@@ -261,13 +261,52 @@ size_t plan_sweep(uint32_t n, int prec, bool ex, uint32_t L, uint32_t Hcap, cons
     g.H = (uint32_t)highs.size();
     for (size_t j = 0; j < highs.size(); j++) g.hpos[j] = highs[j];
     g.ntiles = 1ull << (n - g.L - g.H);
+    // Order of the micro-ops. Exact mode keeps program order (reordering two
+    // gates changes the rounding). Fast mode lets ops on disjoint qubits
+    // commute: one-qubit ops on distinct qubits are emitted back to back, in
+    // runs of up to three, so the kernel applies them in one register pass.
+    std::vector<size_t> order(taken.size());
+    for (size_t t = 0; t < taken.size(); t++) order[t] = t;
+    if (!ex) {
+        const size_t m = taken.size();
+        std::vector<char> done(m, 0);
+        auto ready = [&](size_t i) {
+            for (size_t j = 0; j < i; j++)
+                if (!done[j] && (touch_mask(q[taken[j]]) & touch_mask(q[taken[i]]))) return false;
+            return true;
+        };
+        auto is1q = [&](size_t i) { return q[taken[i]].kind == Q_UNITARY && q[taken[i]].k == 1; };
+        order.clear();
+        while (order.size() < m) {
+            std::vector<size_t> run;  // ready one-qubit ops on distinct qubits, program order
+            uint64_t used = 0;
+            for (size_t i = 0; i < m && run.size() < 3; i++)
+                if (!done[i] && is1q(i) && ready(i) && !((used >> q[taken[i]].qs[0]) & 1)) {
+                    run.push_back(i);
+                    used |= 1ull << q[taken[i]].qs[0];
+                }
+            if (run.size() >= 2) {
+                for (size_t i : run) {
+                    done[i] = 1;
+                    order.push_back(i);
+                }
+                continue;
+            }
+            for (size_t i = 0; i < m; i++)
+                if (!done[i] && ready(i)) {
+                    done[i] = 1;
+                    order.push_back(i);
+                    break;
+                }
+        }
+    }
     std::vector<MicroOp> &mops = plan->mops;
     std::vector<char> &tables = plan->tables;
     mops.assign(taken.size(), MicroOp{});
     tables.clear();
     const size_t es = prec / 8;
     for (size_t t = 0; t < taken.size(); t++) {
-        const QOp &op = q[taken[t]];
+        const QOp &op = q[taken[order[t]]];
         MicroOp &m = mops[t];
         if (op.kind == Q_UNITARY) {
             m.kind = MOP_U1;

@@ -38,10 +38,15 @@ HBM_FALLBACK_GBS = 6800.0
 MEASURED_TRAFFIC_RATIO = {"sweep": (1.075e9 + 1.023e9) / 2.147e9}
 # The same capture: issue slots 73% busy, FMA pipe 58%, FP64 pipe 0%.
 SWEEP_DF_PIPES = {"issue_active_pct": 73.0, "fma_pipe_pct": 58.0, "fp64_pipe_pct": 0.0}
-# Double-float arithmetic of one 2x2 gate: four dot products of four products
-# (df_dot4: 4 x 4 FP32 instructions for the products, 3 TwoSums of 6, 7 adds,
-# 3 to renormalise = 44 per output component) = 176 per amplitude pair.
-DF_FP32_INSTR_PER_AMP_1Q = 88
+# FP32 instructions per amplitude of each double-float sweep micro-op
+# (zeno_gb300/csrc/zc_arith.cuh): a product is 4 (FMUL + 3 FFMA), TwoSum 6,
+# renormalisation 3. Complex 2x2: four 4-term dot products per pair
+# (4*4 + 3*6 + 6 + 3 = 43 each) = 86; real 2x2 and diagonals: 2-term dot
+# products (2*4 + 6 + 2 + 3 = 19), two per amplitude = 38; rotation
+# [[1, -t], [t, 1]]: x + t*y (4 + 6 + 2 + 3 = 15), two per amplitude = 30.
+# CX and SWAP move data only.
+DF_FP32_INSTR_PER_AMP = {"complex": 86, "diag1": 38, "diag_table": 38, "cx": 0, "swap": 0, "real": 38,
+                         "rotation": 30}
 FP32_INSTR_PEAK = 34.3e12  # measured FMA issue rate (zeno_gb300/probes/fp_peaks.cu)
 
 
@@ -341,7 +346,8 @@ def main():
     be.profile(False)
     value, elapsed = job_throughput(a.steps, elapsed, ws)
     gates_ms = sum(d["ms"] for d in classes.values())  # all of our kernels in the timed region
-    n1q = sum(1 for op in ops if op.kind == zc.OP_UNITARY and len(op.qubits) == 1)
+    mops = {k: c1["micro_ops"][k] - c0["micro_ops"][k] for k in c1["micro_ops"]}
+    fp32_instr = sum(n * DF_FP32_INSTR_PER_AMP[k] for k, n in mops.items()) * float(1 << a.qubits)
     dom = max(classes, key=lambda c: classes[c]["ms"])
     dd = classes[dom]
     peak, peak_kind = peaks()
@@ -371,13 +377,14 @@ def main():
                                  "arithmetic; ncu at 26q: %s" % SWEEP_DF_PIPES)
                      if dom == "sweep" and a.mode == "fast" and a.precision == 64 else None,
                      "compute": ({"bound": "fp32_pipe", "unit": "FP32 instr/s",
-                                  "achieved": n1q * a.steps * DF_FP32_INSTR_PER_AMP_1Q * (1 << a.qubits) / (dd["ms"] / 1e3),
+                                  "achieved": fp32_instr / (dd["ms"] / 1e3),
                                   "peak": FP32_INSTR_PEAK,
-                                  "frac": n1q * a.steps * DF_FP32_INSTR_PER_AMP_1Q * (1 << a.qubits) / (dd["ms"] / 1e3)
-                                  / FP32_INSTR_PEAK,
-                                  "count": "one-qubit gates x 88 FP32 instructions per amplitude (double-float "
-                                           "2x2 update); CX/SWAP moves and f64 <-> double-float conversions not "
-                                           "counted"})
+                                  "frac": fp32_instr / (dd["ms"] / 1e3) / FP32_INSTR_PEAK,
+                                  "micro_ops": mops,
+                                  "count": "sweep micro-ops issued in the timed steps x FP32 instructions per "
+                                           "amplitude of their double-float arithmetic %s; index arithmetic, "
+                                           "data moves and f64 <-> double-float conversions not counted"
+                                           % DF_FP32_INSTR_PER_AMP})
                      if dom == "sweep" and a.mode == "fast" and a.precision == 64 else None},
         "clocks": clk.summary(),
     }

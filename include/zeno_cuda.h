@@ -126,6 +126,8 @@ typedef struct {
     uint64_t launches;       /* kernels launched */
     uint64_t sweeps;         /* full-state passes issued by gate kernels */
     uint64_t bytes_moved;    /* algorithmic HBM bytes of those passes */
+    uint64_t micro_ops[8];   /* ops inside multi-op sweeps, by kind: 1 complex 2x2, 2 one-qubit
+                                diagonal, 3 table diagonal, 4 CX, 5 SWAP, 6 real 2x2, 7 rotation */
 } zc_counters;
 int zc_get_counters(zc_state *st, zc_counters *out);
 

@@ -49,7 +49,11 @@ class ZenoCudaError(RuntimeError):
 
 
 class Counters(C.Structure):
-    _fields_ = [("ops", C.c_uint64), ("launches", C.c_uint64), ("sweeps", C.c_uint64), ("bytes_moved", C.c_uint64)]
+    _fields_ = [("ops", C.c_uint64), ("launches", C.c_uint64), ("sweeps", C.c_uint64), ("bytes_moved", C.c_uint64),
+                ("micro_ops", C.c_uint64 * 8)]
+
+# Sweep micro-op kinds (zc_counters.micro_ops index).
+MICRO_OP_KINDS = {1: "complex", 2: "diag1", 3: "diag_table", 4: "cx", 5: "swap", 6: "real", 7: "rotation"}
 
 
 class KernelStat(C.Structure):
@@ -274,7 +278,9 @@ class CudaBackend:
     def counters(self) -> Dict[str, int]:
         c = Counters()
         _check(load().zc_get_counters(self._h, C.byref(c)))
-        return {f: getattr(c, f) for f, _ in Counters._fields_}
+        out = {f: getattr(c, f) for f, _ in Counters._fields_ if f != "micro_ops"}
+        out["micro_ops"] = {name: int(c.micro_ops[k]) for k, name in MICRO_OP_KINDS.items()}
+        return out
 
     def profile(self, enable: bool = True) -> None:
         """Start (and clear) or stop per-launch CUDA-event recording."""

@@ -225,7 +225,13 @@ size_t plan_sweep(uint32_t n, int prec, bool ex, uint32_t L, uint32_t Hcap, cons
     std::vector<size_t> &taken = plan->taken;
     taken.clear();
     const size_t window = std::min(q.size(), kQueueWindow);
-    for (size_t i = 0; i < window && taken.size() < (size_t)kMaxMicroOps; i++) {
+    // Under double-float lowering a diagonal joins the pending tables and
+    // becomes a micro-op only when flushed, so it does not count against the
+    // micro-op budget here (the lowered count is checked below).
+    const bool df_lowering = !ex && prec == 64;
+    size_t counted = 0;
+    for (size_t i = 0; i < window && counted < (size_t)kMaxMicroOps && taken.size() < 4 * (size_t)kMaxMicroOps;
+         i++) {
         const QOp &op = q[i];
         const uint64_t touch = touch_mask(op);
         const bool arith = op.kind == Q_UNITARY || op.kind == Q_DIAG;
@@ -243,6 +249,7 @@ size_t plan_sweep(uint32_t n, int prec, bool ex, uint32_t L, uint32_t Hcap, cons
         highs_mask |= need;
         nhigh += (uint32_t)__builtin_popcountll(need);
         taken.push_back(i);
+        counted += !(df_lowering && op.kind == Q_DIAG);
     }
     if (taken.size() <= 1) return taken.size();
     // pad the tile with further high qubits up to the cap (no effect on results)
@@ -264,7 +271,13 @@ size_t plan_sweep(uint32_t n, int prec, bool ex, uint32_t L, uint32_t Hcap, cons
     // Order of the micro-ops. Exact mode keeps program order (reordering two
     // gates changes the rounding). Fast mode lets ops on disjoint qubits
     // commute: one-qubit ops on distinct qubits are emitted back to back, in
-    // runs of up to three, so the kernel applies them in one register pass.
+    // runs the size of the kernel's register groups (three for f32 states
+    // and for the rotations of lowered f64 sweeps, else two), so the kernel
+    // applies each run in one register pass.
+    const size_t run_cap = prec == 64 && !df_lowering ? 2 : 3;
+    const bool df = df_lowering;
+    std::vector<LoweredOp> low;
+    for (;;) {
     std::vector<size_t> order(taken.size());
     for (size_t t = 0; t < taken.size(); t++) order[t] = t;
     if (!ex) {
@@ -280,65 +293,110 @@ size_t plan_sweep(uint32_t n, int prec, bool ex, uint32_t L, uint32_t Hcap, cons
         while (order.size() < m) {
             std::vector<size_t> run;  // ready one-qubit ops on distinct qubits, program order
             uint64_t used = 0;
-            for (size_t i = 0; i < m && run.size() < 3; i++)
+            for (size_t i = 0; i < m && run.size() < run_cap; i++)
                 if (!done[i] && is1q(i) && ready(i) && !((used >> q[taken[i]].qs[0]) & 1)) {
                     run.push_back(i);
                     used |= 1ull << q[taken[i]].qs[0];
                 }
-            if (run.size() >= 2) {
-                for (size_t i : run) {
-                    done[i] = 1;
-                    order.push_back(i);
-                }
-                continue;
+            // a full run goes out at once; otherwise a ready op of another
+            // kind goes first (it can make more one-qubit ops ready), and a
+            // short run only when nothing else is ready
+            bool emitted = false;
+            if (run.size() < run_cap)
+                for (size_t i = 0; i < m && !emitted; i++)
+                    if (!done[i] && !is1q(i) && ready(i)) {
+                        done[i] = 1;
+                        order.push_back(i);
+                        emitted = true;
+                    }
+            if (emitted) continue;
+            for (size_t i : run) {
+                done[i] = 1;
+                order.push_back(i);
             }
-            for (size_t i = 0; i < m; i++)
-                if (!done[i] && ready(i)) {
-                    done[i] = 1;
-                    order.push_back(i);
-                    break;
-                }
         }
+    }
+    // Lowering: double-float sweeps of f64 states rewrite one-qubit gates as
+    // diagonal * real * diagonal and merge the diagonals; other policies
+    // encode the ops as they are.
+    low.clear();
+    plan->carry.clear();
+    if (df) {
+        std::vector<const QOp *> seq;
+        for (size_t t : order) seq.push_back(&q[taken[t]]);
+        lower_df(seq, 2, &low, &plan->carry);
+    } else {
+        for (size_t t : order) {
+            const QOp &op = q[taken[t]];
+            LoweredOp o{};
+            if (op.kind == Q_UNITARY) {
+                o.kind = MOP_U1;
+                o.a = op.qs[0];
+                for (int i = 0; i < 8; i++) o.m[i] = op.data[i];
+            } else if (op.kind == Q_DIAG) {
+                o.kind = MOP_DK;
+                o.sup.assign(op.qs, op.qs + op.k);
+                o.tab = op.data;
+            } else {
+                o.kind = op.kind == Q_CX ? MOP_CX : MOP_SWAP;
+                o.a = op.a;
+                o.b = op.b;
+            }
+            low.push_back(std::move(o));
+        }
+    }
+    if (low.size() <= (size_t)kMaxMicroOps) break;
+    // lowering added table ops: take fewer queue ops (dropping the last
+    // taken op never breaks an ordering constraint)
+    taken.pop_back();
+    if (taken.size() <= 1) {
+        plan->carry.clear();
+        return taken.size();
+    }
     }
     std::vector<MicroOp> &mops = plan->mops;
     std::vector<char> &tables = plan->tables;
-    mops.assign(taken.size(), MicroOp{});
+    mops.assign(low.size(), MicroOp{});
     tables.clear();
     const size_t es = prec / 8;
-    for (size_t t = 0; t < taken.size(); t++) {
-        const QOp &op = q[taken[order[t]]];
+    for (size_t t = 0; t < low.size(); t++) {
+        const LoweredOp &op = low[t];
         MicroOp &m = mops[t];
-        if (op.kind == Q_UNITARY) {
-            m.kind = MOP_U1;
-            m.a = loc_of(op.qs[0], g.L, highs);
-            for (int i = 0; i < 8; i++) m.m[i] = op.data[i];
-        } else if (op.kind == Q_DIAG && op.k == 1) {
+        if (op.kind == MOP_U1 || op.kind == MOP_R1 || op.kind == MOP_RT) {
+            m.kind = op.kind;
+            m.a = loc_of(op.a, g.L, highs);
+            if (op.kind == MOP_RT) m.b = op.b;  // form
+            for (int i = 0; i < 8; i++) m.m[i] = op.m[i];
+        } else if (op.kind == MOP_DK && op.sup.size() == 1 && !df) {  // double-float: tables ride in groups
             m.kind = MOP_D1;
-            m.a = loc_of(op.qs[0], g.L, highs);
-            for (int i = 0; i < 4; i++) m.m[i] = op.data[i];
-        } else if (op.kind == Q_DIAG) {
+            m.a = loc_of(op.sup[0], g.L, highs);
+            for (int i = 0; i < 4; i++) m.m[i] = op.tab[i];
+        } else if (op.kind == MOP_DK) {
             m.kind = MOP_DK;
-            m.k = op.k;
-            for (uint32_t b = 0; b < op.k; b++) m.loc[b] = loc_of(op.qs[b], g.L, highs);
-            const size_t dim = (size_t)1 << op.k;
+            m.k = (uint32_t)op.sup.size();
+            for (uint32_t b = 0; b < m.k; b++) m.loc[b] = loc_of(op.sup[b], g.L, highs);
+            const size_t dim = (size_t)1 << m.k;
             size_t off = (tables.size() + 15) & ~(size_t)15;
             tables.resize(off + 2 * dim * es);
             for (size_t j = 0; j < dim; j++) {
-                if (es == 8) {
-                    ((double *)(tables.data() + off))[j] = op.data[2 * j];
-                    ((double *)(tables.data() + off))[dim + j] = op.data[2 * j + 1];
+                const double xr = op.tab[2 * j], xi = op.tab[2 * j + 1];
+                if (df) {  // (re hi, re lo, im hi, im lo)
+                    float *e = (float *)(tables.data() + off) + 4 * j;
+                    e[0] = (float)xr;
+                    e[1] = (float)(xr - (double)e[0]);
+                    e[2] = (float)xi;
+                    e[3] = (float)(xi - (double)e[2]);
+                } else if (es == 8) {
+                    ((double *)(tables.data() + off))[j] = xr;
+                    ((double *)(tables.data() + off))[dim + j] = xi;
                 } else {
-                    ((float *)(tables.data() + off))[j] = (float)op.data[2 * j];
-                    ((float *)(tables.data() + off))[dim + j] = (float)op.data[2 * j + 1];
+                    ((float *)(tables.data() + off))[j] = (float)xr;
+                    ((float *)(tables.data() + off))[dim + j] = (float)xi;
                 }
             }
             m.table = off;
-        } else if (op.kind == Q_CX) {
-            m.kind = MOP_CX;
-            m.a = loc_of(op.a, g.L, highs);
-            m.b = loc_of(op.b, g.L, highs);
         } else {
-            m.kind = MOP_SWAP;
+            m.kind = op.kind;
             m.a = loc_of(op.a, g.L, highs);
             m.b = loc_of(op.b, g.L, highs);
         }
@@ -359,6 +417,17 @@ void erase_taken(std::vector<QOp> &q, const std::vector<size_t> &taken) {
         rest.push_back(std::move(q[i]));
     }
     q.swap(rest);
+}
+
+// The carried diagonals act after every op the sweep took and touch only
+// qubits those ops touched; no op deferred ahead of them touches those qubits,
+// so the queue front is their place in program order.
+void consume_plan(std::vector<QOp> &q, SweepPlan &plan) {
+    erase_taken(q, plan.taken);
+    if (!plan.carry.empty()) {
+        q.insert(q.begin(), std::make_move_iterator(plan.carry.begin()), std::make_move_iterator(plan.carry.end()));
+        plan.carry.clear();
+    }
 }
 
 // Plan and launch one sweep starting at the queue front; erases what ran.
@@ -382,7 +451,8 @@ static int run_one_sweep(zc_state *st) {
     if (rc) return rc;
     rc = launch_sweep(st, plan.g, (const MicroOp *)dev, (int)plan.mops.size(), (const char *)dev + tab_off,
                       exact(st));
-    erase_taken(q, plan.taken);
+    for (const MicroOp &m : plan.mops) st->ctr.micro_ops[m.kind & 7]++;
+    consume_plan(q, plan);
     return rc;
 }
 

@@ -244,6 +244,67 @@ __device__ __forceinline__ void pair_update_df(const MatDF &m, float2 &ar, float
     bi = nbi;
 }
 
+// Real 2x2 update (r00 r01 r10 r11) of (a, b) in double-float: four
+// two-term dot products instead of the complex update's four-term ones.
+__device__ __forceinline__ void pair_update_rdf(const float2 *r, float2 &ar, float2 &ai, float2 &br, float2 &bi) {
+    const float2 nar = df_dot2(r[0], ar, r[1], br);
+    const float2 nai = df_dot2(r[0], ai, r[1], bi);
+    const float2 nbr = df_dot2(r[2], ar, r[3], br);
+    const float2 nbi = df_dot2(r[2], ai, r[3], bi);
+    ar = nar;
+    ai = nai;
+    br = nbr;
+    bi = nbi;
+}
+
+// x + t*y in double-float (one product, one TwoSum).
+__device__ __forceinline__ float2 df_axpy(float2 x, float2 t, float2 y) {
+    float p, e, r;
+    df_prod(t, y, p, e);
+    const float s = two_sum(x.x, p, r);
+    return df_norm(s, __fadd_rn(x.y, __fadd_rn(e, r)));
+}
+
+// Rotation update of (a, b) with unit diagonal: [[1, -t], [t, 1]]
+// (|t| <= 1; the scale that makes it orthogonal lives in a diagonal).
+__device__ __forceinline__ void pair_update_rot_df(float2 t, float2 &ar, float2 &ai, float2 &br, float2 &bi) {
+    const float2 nt = df_neg(t);
+    const float2 nar = df_axpy(ar, nt, br);
+    const float2 nai = df_axpy(ai, nt, bi);
+    const float2 nbr = df_axpy(br, t, ar);
+    const float2 nbi = df_axpy(bi, t, ai);
+    ar = nar;
+    ai = nai;
+    br = nbr;
+    bi = nbi;
+}
+
+// The same rotation in T (FMA-contracted).
+template <typename T>
+__device__ __forceinline__ void pair_update_rot(T t, T &ar, T &ai, T &br, T &bi) {
+    const T nar = rfma(-t, br, ar);
+    const T nai = rfma(-t, bi, ai);
+    const T nbr = rfma(t, ar, br);
+    const T nbi = rfma(t, ai, bi);
+    ar = nar;
+    ai = nai;
+    br = nbr;
+    bi = nbi;
+}
+
+// The same real update in T (FMA-contracted).
+template <typename T>
+__device__ __forceinline__ void pair_update_real(const T *r, T &ar, T &ai, T &br, T &bi) {
+    const T nar = rfma(r[0], ar, rmul(r[1], br));
+    const T nai = rfma(r[0], ai, rmul(r[1], bi));
+    const T nbr = rfma(r[2], ar, rmul(r[3], br));
+    const T nbi = rfma(r[2], ai, rmul(r[3], bi));
+    ar = nar;
+    ai = nai;
+    br = nbr;
+    bi = nbi;
+}
+
 __device__ __forceinline__ void cscale_df(float2 wr, float2 wi, float2 &ar, float2 &ai) {
     const float2 nr = df_dot2(wr, ar, df_neg(wi), ai);
     const float2 ni = df_dot2(wr, ai, wi, ar);

@@ -140,10 +140,29 @@ struct SweepPlan {
     std::vector<MicroOp> mops;
     std::vector<char> tables;
     std::vector<size_t> taken;
+    std::vector<QOp> carry;  // diagonals left pending by the sweep: they go to the queue front
 };
 size_t plan_sweep(uint32_t n, int prec, bool ex, uint32_t L, uint32_t Hcap, const std::vector<QOp> &q,
                   SweepPlan *plan);
 void erase_taken(std::vector<QOp> &q, const std::vector<size_t> &taken);
+// Remove the plan's ops from the queue and put its carried diagonals in front.
+void consume_plan(std::vector<QOp> &q, SweepPlan &plan);
+
+// A sweep op in global qubits before encoding (kind: MOP_*). DK: ascending
+// support `sup` and an interleaved complex table over it.
+struct LoweredOp {
+    uint32_t kind = 0;
+    uint32_t a = 0, b = 0;
+    double m[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    std::vector<uint32_t> sup;
+    std::vector<double> tab;
+};
+// Double-float lowering of a fast f64 sweep: one-qubit gates as diagonal *
+// real * diagonal, the diagonals propagated and merged into table ops placed
+// before the register runs of at most run_cap gates. Pending diagonals at the
+// end go to *carry (when it is given and the sequence has a non-diagonal op).
+void lower_df(const std::vector<const QOp *> &seq, int run_cap, std::vector<LoweredOp> *out,
+              std::vector<QOp> *carry);
 int launch_single(zc_state *st, const QOp &op);
 int launch_sweep_multi(cudaStream_t stream, int num_sms, int prec, bool exact, const char *dev_blob, int *d_err);
 int arena_put(zc_state *st, const void *src, size_t bytes, const void **dev);

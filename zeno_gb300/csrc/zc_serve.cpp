@@ -257,7 +257,7 @@ int packed_step(zc_server *s, int gi, int round, int *issued) {
     s->packed_launches++;
     g.launches++;
     (*issued)++;
-    for (auto &pr : planned) erase_taken(pr.first->queue, pr.second.taken);
+    for (auto &pr : planned) consume_plan(pr.first->queue, pr.second);
     return ZC_OK;
 }
 

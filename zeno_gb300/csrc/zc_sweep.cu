@@ -83,6 +83,32 @@ struct OpCoef {
     typename std::conditional<A == AR_DF, float2, T>::type v[8];
 };
 
+__device__ __forceinline__ bool is_1q(uint32_t kind) { return kind == MOP_U1 || kind == MOP_R1 || kind == MOP_RT; }
+
+// The register group starting at one-qubit op o: three rotations on distinct
+// bits (f64 states outside FMA mode, whose other groups are two), else up to
+// kMaxGroup one-qubit ops on distinct bits. Returns its size; *rot3 tells the
+// first kind.
+template <typename T, int A>
+__device__ __forceinline__ int group_at(const MicroOp *ops, int o, int nops, bool *rot3) {
+    constexpr int kMaxGroup = sizeof(T) == 8 && A != AR_FMA ? 2 : 3;
+    *rot3 = false;
+    if (kMaxGroup == 2 && o + 2 < nops && ops[o].kind == MOP_RT && ops[o + 1].kind == MOP_RT &&
+        ops[o + 2].kind == MOP_RT && ops[o].a != ops[o + 1].a && ops[o].a != ops[o + 2].a &&
+        ops[o + 1].a != ops[o + 2].a) {
+        *rot3 = true;
+        return 3;
+    }
+    int g = 1;
+    while (g < kMaxGroup && o + g < nops && is_1q(ops[o + g].kind)) {
+        bool distinct = true;
+        for (int h = 0; h < g; h++) distinct &= ops[o + h].a != ops[o + g].a;
+        if (!distinct) break;
+        g++;
+    }
+    return g;
+}
+
 template <typename R>
 __device__ __forceinline__ uint32_t jgather(const MicroOp &op, uint32_t jo, uint32_t v) {
     uint32_t j = jo;
@@ -98,12 +124,18 @@ __device__ __forceinline__ uint32_t jouter(const MicroOp &op, uint64_t base) {
     return jo;
 }
 
-// Apply G consecutive one-qubit micro-ops (ops[o..o+G), distinct tile bits)
-// to register-held groups of 2^G elements: each gate updates the same pairs
-// with the same arithmetic, in the same order, as one op at a time.
-template <typename T, int A, typename R, int G>
+// Apply G consecutive one-qubit micro-ops (U1, R1 or RT; only RT when
+// ROT_ONLY; ops[o..o+G), distinct tile bits) to register-held groups of 2^G
+// elements: each gate updates the same pairs with the same arithmetic, in the
+// same order, as one op at a time. The pair swaps of flipped RT ops commute
+// with the group's other gates (other bits), so they all happen at the store:
+// element e goes to the slot of e ^ flips. With FUSE_DK the table diagonal
+// `dk` (the op just before the group, double-float tables) scales each
+// element first, exactly as its own pass would.
+template <typename T, int A, typename R, int G, bool ROT_ONLY = false, bool FUSE_DK = false>
 __device__ void apply_u1_group(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *coef, int o, uint32_t size,
-                               uint32_t *bad) {
+                               uint32_t *bad, const MicroOp *dk = nullptr, const char *tables = nullptr,
+                               uint64_t base = 0) {
     constexpr int E = 1 << G;
     uint32_t bits[G], sorted[G];
 #pragma unroll
@@ -117,29 +149,99 @@ __device__ void apply_u1_group(R *sr, R *si, const MicroOp *ops, const OpCoef<T,
                 sorted[j] = sorted[j - 1];
                 sorted[j - 1] = x;
             }
+    uint32_t flips = 0, bad_bit = 0;
+#pragma unroll
+    for (int g = 0; g < G; g++) {
+        if (ops[o + g].kind == MOP_RT && ops[o + g].b) flips |= 1u << g;
+        if ((1u << bits[g]) >= size) bad_bit = bits[g];
+    }
+    // every slot is inside the tile when the bits are (v < size / 2^G with
+    // G zero bits inserted below log2(size)); a bad bit is recorded and the
+    // group skipped
+    if (bad_bit) {
+        if (threadIdx.x == 0) *bad = bad_bit | 0x80000000u;
+        return;
+    }
+    // flipped elements: slot(e ^ flips) = slot(e) ^ fmask
+    uint32_t fmask = 0;
+#pragma unroll
+    for (int g = 0; g < G; g++) fmask |= ((flips >> g) & 1u) << bits[g];
+    // fused diagonal: element e of the group reads table entry jb(v) ^ tp(e),
+    // jb from the support bits outside the group, tp from the group's bits
+    uint32_t jo = 0, tb[G];
+    const float4 *dtab = nullptr;
+    if constexpr (FUSE_DK) {
+        jo = jouter(*dk, base);
+        dtab = reinterpret_cast<const float4 *>(tables + dk->table);
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            tb[g] = 0;
+            for (uint32_t b = 0; b < dk->k; b++)
+                if (dk->loc[b] == bits[g]) tb[g] = 1u << b;
+        }
+    }
     for (uint32_t p = threadIdx.x; p < size / E; p += blockDim.x) {
         uint32_t v = p;
 #pragma unroll
         for (int g = 0; g < G; g++) v = ((v >> sorted[g]) << (sorted[g] + 1)) | (v & ((1u << sorted[g]) - 1));
-        uint32_t idx[E];
-        R xr[E], xi[E];
-#pragma unroll
-        for (int e = 0; e < E; e++) {
+        // element e of the group sits at v | (bits selected by e)
+        // (recomputed at the store so the indices need no registers across
+        // the arithmetic)
+        auto slot = [&](uint32_t e) {
             uint32_t w = v;
 #pragma unroll
             for (int g = 0; g < G; g++)
-                if ((e >> g) & 1) w |= 1u << bits[g];
-            if (w >= size) {  // cannot happen for tile bits < log2(size); recorded, access skipped
-                *bad = w | 0x80000000u;
-                w = 0;
-            }
-            idx[e] = w;
+                if ((e >> g) & 1u) w ^= 1u << bits[g];
+            return w;
+        };
+        R xr[E], xi[E];
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            const uint32_t w = slot(e);
             xr[e] = sr[w];
             xi[e] = si[w];
         }
+        if constexpr (FUSE_DK) {
+            uint32_t jb = jo;
+            for (uint32_t b = 0; b < dk->k; b++) {
+                const uint32_t l = dk->loc[b];
+                if (!(l & kOuterFlag)) jb |= ((v >> l) & 1u) << b;
+            }
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+                uint32_t j = jb;
+#pragma unroll
+                for (int g = 0; g < G; g++)
+                    if ((e >> g) & 1) j ^= tb[g];
+                const float4 w = __ldg(dtab + j);
+                cscale_df(make_float2(w.x, w.y), make_float2(w.z, w.w), xr[e], xi[e]);
+            }
+        }
 #pragma unroll
         for (int g = 0; g < G; g++) {
-            if constexpr (A == AR_DF) {
+            if (ROT_ONLY || ops[o + g].kind == MOP_RT) {
+                const R t = coef[o + g].v[0];
+#pragma unroll
+                for (int e = 0; e < E; e++)
+                    if (!((e >> g) & 1)) {
+                        if constexpr (A == AR_DF)
+                            pair_update_rot_df(t, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                        else
+                            pair_update_rot<T>(t, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                    }
+            } else if (ops[o + g].kind == MOP_R1) {
+                R r[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) r[i] = coef[o + g].v[i];
+#pragma unroll
+                for (int e = 0; e < E; e++)
+                    if (!((e >> g) & 1)) {
+                        if constexpr (A == AR_DF)
+                            pair_update_rdf(r, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                        else
+                            pair_update_real<T>(r, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                    }
+            } else if constexpr (A == AR_DF) {
                 MatDF m;
 #pragma unroll
                 for (int i = 0; i < 8; i++) m.v[i] = coef[o + g].v[i];
@@ -156,10 +258,12 @@ __device__ void apply_u1_group(R *sr, R *si, const MicroOp *ops, const OpCoef<T,
                         pair_update<T, A == AR_EXACT>(m, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
             }
         }
+        v ^= fmask;
 #pragma unroll
         for (int e = 0; e < E; e++) {
-            sr[idx[e]] = xr[e];
-            si[idx[e]] = xi[e];
+            const uint32_t w = slot((uint32_t)e);
+            sr[w] = xr[e];
+            si[w] = xi[e];
         }
     }
 }
@@ -172,17 +276,34 @@ __device__ void apply_ops(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int o = 0; o < nops; o++) {
         const MicroOp &op = ops[o];
-        if (op.kind == MOP_U1) {
+        if constexpr (A == AR_DF) {
+            // a table diagonal right before a register group rides in its pass
+            if (op.kind == MOP_DK && o + 1 < nops && is_1q(ops[o + 1].kind)) {
+                bool rot3;
+                const int g = group_at<T, A>(ops, o + 1, nops, &rot3);
+                if (rot3)
+                    apply_u1_group<T, A, R, 3, true, true>(sr, si, ops, coef, o + 1, size, bad, &op, tables, base);
+                else if (g == 2)
+                    apply_u1_group<T, A, R, 2, false, true>(sr, si, ops, coef, o + 1, size, bad, &op, tables, base);
+                else
+                    apply_u1_group<T, A, R, 1, false, true>(sr, si, ops, coef, o + 1, size, bad, &op, tables, base);
+                o += g;
+                __syncthreads();
+                continue;
+            }
+        }
+        if (is_1q(op.kind)) {
             // runs of up to three one-qubit ops on distinct bits share one
             // register pass (two for f64 states outside FMA mode, which would
-            // spill at the 80-register cap with three)
+            // spill at the 80-register cap with three, except for rotations)
             constexpr int kMaxGroup = sizeof(T) == 8 && A != AR_FMA ? 2 : 3;
-            int g = 1;
-            while (g < kMaxGroup && o + g < nops && ops[o + g].kind == MOP_U1) {
-                bool distinct = true;
-                for (int h = 0; h < g; h++) distinct &= ops[o + h].a != ops[o + g].a;
-                if (!distinct) break;
-                g++;
+            bool rot3;
+            const int g = group_at<T, A>(ops, o, nops, &rot3);
+            if (rot3) {
+                apply_u1_group<T, A, R, 3, true>(sr, si, ops, coef, o, size, bad);
+                o += 2;
+                __syncthreads();
+                continue;
             }
             if (kMaxGroup == 3 && g == 3) {
                 apply_u1_group<T, A, R, kMaxGroup>(sr, si, ops, coef, o, size, bad);
@@ -197,6 +318,34 @@ __device__ void apply_ops(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *
                 continue;
             }
             const uint32_t b = op.a;
+            if (op.kind == MOP_RT) {
+                const R t = coef[o].v[0];
+                const uint32_t flip = op.b ? 1u << b : 0u;
+                for (uint32_t p = tid; p < size / 2; p += nt) {
+                    const uint32_t v0 = ((p >> b) << (b + 1)) | (p & ((1u << b) - 1)), v1 = v0 | (1u << b);
+                    R ar = sr[v0], ai = si[v0], br = sr[v1], bi = si[v1];
+                    if constexpr (A == AR_DF) pair_update_rot_df(t, ar, ai, br, bi);
+                    else pair_update_rot<T>(t, ar, ai, br, bi);
+                    sr[v0 ^ flip] = ar;
+                    si[v0 ^ flip] = ai;
+                    sr[v1 ^ flip] = br;
+                    si[v1 ^ flip] = bi;
+                }
+                __syncthreads();
+                continue;
+            }
+            if (op.kind == MOP_R1) {
+                R r[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) r[i] = coef[o].v[i];
+                for (uint32_t p = tid; p < size / 2; p += nt) {
+                    const uint32_t v0 = ((p >> b) << (b + 1)) | (p & ((1u << b) - 1)), v1 = v0 | (1u << b);
+                    if constexpr (A == AR_DF) pair_update_rdf(r, sr[v0], si[v0], sr[v1], si[v1]);
+                    else pair_update_real<T>(r, sr[v0], si[v0], sr[v1], si[v1]);
+                }
+                __syncthreads();
+                continue;
+            }
             typename std::conditional<A == AR_DF, MatDF, Mat2<T>>::type m;
 #pragma unroll
             for (int i = 0; i < 8; i++) m.v[i] = coef[o].v[i];
@@ -236,25 +385,34 @@ __device__ void apply_ops(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *
             const uint32_t jo = jouter(op, base);
             const T *dre = reinterpret_cast<const T *>(tables + op.table);
             const T *dim_ = dre + (1u << op.k);
+            const float4 *dtab = reinterpret_cast<const float4 *>(tables + op.table);  // double-float entries
             // table index of element v = jo | lut[v & 255] | lut[256 + (v >> 8)]:
             // the op's local bits gathered once per op instead of per element
             for (uint32_t x = tid; x < 256 + kJlutHigh; x += nt)
                 jlut[x] = (uint16_t)jgather<R>(op, 0u, x < 256 ? x : (x - 256) << 8);
             __syncthreads();
-            auto scl = [&](T wr, T wi, R &xr, R &xi) {
-                if constexpr (A == AR_DF) cscale_df(df_from_f64(wr), df_from_f64(wi), xr, xi);
+            // W: the table entry (T re, T im; or one float4 of double-float pairs)
+            using W = typename std::conditional<A == AR_DF, float4, T>::type;
+            auto load_w = [&](uint32_t j, W &wr, W &wi) {
+                if constexpr (A == AR_DF) wr = __ldg(dtab + j);
+                else {
+                    wr = __ldg(dre + j);
+                    wi = __ldg(dim_ + j);
+                }
+            };
+            auto scl = [&](const W &wr, const W &wi, R &xr, R &xi) {
+                if constexpr (A == AR_DF) cscale_df(make_float2(wr.x, wr.y), make_float2(wr.z, wr.w), xr, xi);
                 else cscale<T, A == AR_EXACT>(wr, wi, xr, xi);
             };
             uint32_t v = tid;
             for (; v + 3u * nt < size; v += 4u * nt) {
                 R xr[4], xi[4];
-                T wr[4], wi[4];
+                W wr[4], wi[4];
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
                     const uint32_t vk = v + k * nt;
                     const uint32_t j = jo | jlut[vk & 255u] | jlut[256 + (vk >> 8)];
-                    wr[k] = __ldg(dre + j);
-                    wi[k] = __ldg(dim_ + j);
+                    load_w(j, wr[k], wi[k]);
                     xr[k] = sr[vk];
                     xi[k] = si[vk];
                 }
@@ -267,7 +425,9 @@ __device__ void apply_ops(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *
             }
             for (; v < size; v += nt) {
                 const uint32_t j = jo | jlut[v & 255u] | jlut[256 + (v >> 8)];
-                scl(__ldg(dre + j), __ldg(dim_ + j), sr[v], si[v]);
+                W wr, wi;
+                load_w(j, wr, wi);
+                scl(wr, wi, sr[v], si[v]);
             }
         } else {
             apply_perm(sr, si, op, base, size);
@@ -323,8 +483,8 @@ __device__ void load_job(SweepSmem<T, A> &c, const MicroOp *gops, int nops, uint
     __syncthreads();
     if (tid < nops) {
         const MicroOp &op = c.ops[tid];
-        if (op.kind == MOP_U1 || op.kind == MOP_D1) {
-            const int cnt = op.kind == MOP_U1 ? 8 : 4;
+        if (op.kind == MOP_U1 || op.kind == MOP_D1 || op.kind == MOP_R1 || op.kind == MOP_RT) {
+            const int cnt = op.kind == MOP_U1 ? 8 : op.kind == MOP_RT ? 1 : 4;
             for (int i = 0; i < cnt; i++) {
                 if constexpr (A == AR_DF)
                     c.coef[tid].v[i] = df_from_f64(op.m[i]);
@@ -335,7 +495,8 @@ __device__ void load_job(SweepSmem<T, A> &c, const MicroOp *gops, int nops, uint
     }
     if (tid == 0) {
         int ar = 0;
-        for (int o = 0; o < nops; o++) ar |= c.ops[o].kind == MOP_U1 || c.ops[o].kind == MOP_D1 || c.ops[o].kind == MOP_DK;
+        for (int o = 0; o < nops; o++)
+            ar |= c.ops[o].kind != MOP_CX && c.ops[o].kind != MOP_SWAP;
         c.has_arith = ar;
     }
     __syncthreads();

@@ -10,7 +10,7 @@ constexpr int kMaxMicroOps = 32;               // ops per sweep
 constexpr uint32_t kMaxSweepHigh = 7;          // chosen high qubits per tile
 constexpr size_t kSweepSmemBytes = 64 * 1024;  // one tile buffer: 2^12 f64 or 2^13 f32 (re + im)
 
-enum : uint32_t { MOP_U1 = 1, MOP_D1 = 2, MOP_DK = 3, MOP_CX = 4, MOP_SWAP = 5 };
+enum : uint32_t { MOP_U1 = 1, MOP_D1 = 2, MOP_DK = 3, MOP_CX = 4, MOP_SWAP = 5, MOP_R1 = 6, MOP_RT = 7 };
 
 // Tile geometry: local qubits are 0..L-1 plus hpos[0..H) (ascending).
 struct SweepGeom {
@@ -22,8 +22,11 @@ struct SweepGeom {
 // One op inside a sweep, operands as local bit indices (0..L+H) or
 // kOuterFlag | global qubit. U1: a = bit, m = 2x2 row-major (re, im);
 // D1: a = bit, m[0..4) = d0, d1; DK: k, loc[], table = byte offset of
-// [re(2^k) | im(2^k)] in the sweep's table block; CX: a = control,
-// b = target (local); SWAP: a, b local.
+// [re(2^k) | im(2^k)] in the sweep's table block (for double-float sweeps
+// of f64 states: 2^k entries of (re hi, re lo, im hi, im lo) floats);
+// CX: a = control, b = target (local); SWAP: a, b local; R1: a = bit,
+// m[0..4) = real 2x2 r00 r01 r10 r11; RT: a = bit, m[0] = t, b = flip:
+// [[1, -t], [t, 1]], then (flip) the pair's two amplitudes trade places.
 struct MicroOp {
     uint32_t kind, a, b, k;
     uint32_t loc[12];

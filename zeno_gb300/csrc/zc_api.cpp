@@ -290,14 +290,23 @@ size_t plan_sweep(uint32_t n, int prec, bool ex, uint32_t L, uint32_t Hcap, cons
         };
         auto is1q = [&](size_t i) { return q[taken[i]].kind == Q_UNITARY && q[taken[i]].k == 1; };
         order.clear();
+        uint64_t cx_targets = 0;  // targets of the CX ops since the last run
         while (order.size() < m) {
-            std::vector<size_t> run;  // ready one-qubit ops on distinct qubits, program order
+            // ready one-qubit ops on distinct qubits, program order; those on
+            // targets of the CX ops just emitted first (the kernel folds a CX
+            // into the register group that holds its target)
+            std::vector<size_t> run;
             uint64_t used = 0;
-            for (size_t i = 0; i < m && run.size() < run_cap; i++)
-                if (!done[i] && is1q(i) && ready(i) && !((used >> q[taken[i]].qs[0]) & 1)) {
+            for (int pass = 0; pass < 2; pass++)
+                for (size_t i = 0; i < m && run.size() < run_cap; i++) {
+                    if (done[i] || !is1q(i) || !ready(i)) continue;
+                    const uint32_t qb = q[taken[i]].qs[0];
+                    if ((used >> qb) & 1) continue;
+                    if (pass == 0 && !((cx_targets >> qb) & 1)) continue;
                     run.push_back(i);
-                    used |= 1ull << q[taken[i]].qs[0];
+                    used |= 1ull << qb;
                 }
+            std::sort(run.begin(), run.end());
             // a full run goes out at once; otherwise a ready op of another
             // kind goes first (it can make more one-qubit ops ready), and a
             // short run only when nothing else is ready
@@ -308,12 +317,14 @@ size_t plan_sweep(uint32_t n, int prec, bool ex, uint32_t L, uint32_t Hcap, cons
                         done[i] = 1;
                         order.push_back(i);
                         emitted = true;
+                        if (q[taken[i]].kind == Q_CX) cx_targets |= 1ull << q[taken[i]].b;
                     }
             if (emitted) continue;
             for (size_t i : run) {
                 done[i] = 1;
                 order.push_back(i);
             }
+            cx_targets = 0;
         }
     }
     // Lowering: double-float sweeps of f64 states rewrite one-qubit gates as

@@ -196,6 +196,64 @@ struct Item {
     Term diag;  // Q_DIAG
 };
 
+bool cx_commute(const LoweredOp &x, const LoweredOp &y) {
+    // CX(a, b) and CX(c, d) commute unless one's target is the other's control
+    return x.b != y.a && y.b != x.a;
+}
+
+bool is_1q_op(uint32_t kind) { return kind == MOP_U1 || kind == MOP_R1 || kind == MOP_RT; }
+
+// Size of the kernel's register group at out[i] (three rotations on distinct
+// qubits, else up to run_cap one-qubit ops on distinct qubits).
+size_t group_size(const std::vector<LoweredOp> &out, size_t i, int run_cap) {
+    if (i + 2 < out.size() && out[i].kind == MOP_RT && out[i + 1].kind == MOP_RT && out[i + 2].kind == MOP_RT &&
+        out[i].a != out[i + 1].a && out[i].a != out[i + 2].a && out[i + 1].a != out[i + 2].a)
+        return 3;
+    size_t g = 1;
+    while ((int)g < run_cap && i + g < out.size() && is_1q_op(out[i + g].kind)) {
+        bool distinct = true;
+        for (size_t h = 0; h < g; h++) distinct &= out[i + h].a != out[i + g].a;
+        if (!distinct) break;
+        g++;
+    }
+    return g;
+}
+
+// The kernel takes a block of CX ops right before a register group (and its
+// table diagonal) into the group's loads when every target is a group qubit,
+// peeling leading CX ops that do not qualify into their own passes. Move the
+// block's non-qualifying CX ops to its front where they commute with the
+// qualifying ones they pass.
+void arrange_cx_blocks(std::vector<LoweredOp> &out, int run_cap) {
+    for (size_t i = 0; i < out.size();) {
+        if (out[i].kind != MOP_CX) {
+            i++;
+            continue;
+        }
+        size_t j = i;
+        while (j < out.size() && out[j].kind == MOP_CX) j++;
+        const size_t g0 = j < out.size() && out[j].kind == MOP_DK ? j + 1 : j;
+        if (g0 < out.size() && is_1q_op(out[g0].kind)) {
+            const size_t g = group_size(out, g0, run_cap);
+            auto in_group = [&](uint32_t q) {
+                for (size_t h = 0; h < g; h++)
+                    if (out[g0 + h].a == q) return true;
+                return false;
+            };
+            // bubble each non-qualifying CX towards the block front
+            for (size_t k = i; k < j; k++) {
+                if (in_group(out[k].b)) continue;
+                size_t p = k;
+                while (p > i && in_group(out[p - 1].b) && cx_commute(out[p - 1], out[p])) {
+                    std::swap(out[p - 1], out[p]);
+                    p--;
+                }
+            }
+        }
+        i = j;
+    }
+}
+
 }  // namespace
 
 void lower_df(const std::vector<const QOp *> &seq, int run_cap, std::vector<LoweredOp> *out,
@@ -318,6 +376,7 @@ void lower_df(const std::vector<const QOp *> &seq, int run_cap, std::vector<Lowe
         }
         i++;
     }
+    arrange_cx_blocks(*out, run_cap);
     if (carry && has_non_diag) {
         for (const Term &t : pending) {
             const LoweredOp d = diag_op(t);

@@ -26,6 +26,18 @@ namespace {
 constexpr int kSweepThreads = 256;
 constexpr int kSweepCtasPerSm = 3;
 constexpr uint32_t kJlutHigh = 1u << (13 - 8);  // tile index values above the low byte (tiles <= 2^13)
+constexpr int kMaxFoldCx = 4;                   // CX ops one register group takes into its loads
+
+// The part of a MicroOp the tile loop reads (its first 72 bytes); the matrix
+// entries are read once per job, from global memory, into the coefficients.
+struct OpHead {
+    uint32_t kind, a, b, k;
+    uint32_t loc[12];
+    uint64_t table;
+};
+static_assert(sizeof(OpHead) == 72 && offsetof(MicroOp, table) == offsetof(OpHead, table) &&
+                  offsetof(MicroOp, m) == sizeof(OpHead),
+              "OpHead is the head of MicroOp");
 // Global index of the first element of tile t: the tile number fills the
 // non-local positions above the L low bits.
 __device__ __forceinline__ uint64_t tile_base(uint64_t t, uint32_t L, const uint32_t *hpos, uint32_t H) {
@@ -46,7 +58,7 @@ __device__ __forceinline__ void swap_slots(T *sr, T *si, uint32_t v0, uint32_t v
 // Permutation micro-ops (CX, SWAP) move raw slots, so they serve every
 // arithmetic policy and representation.
 template <typename T>
-__device__ void apply_perm(T *sr, T *si, const MicroOp &op, uint64_t base, uint32_t size) {
+__device__ void apply_perm(T *sr, T *si, const OpHead &op, uint64_t base, uint32_t size) {
     const int tid = threadIdx.x, nt = blockDim.x;
     if (op.kind == MOP_CX) {
         const uint32_t t = op.b;
@@ -90,7 +102,7 @@ __device__ __forceinline__ bool is_1q(uint32_t kind) { return kind == MOP_U1 || 
 // kMaxGroup one-qubit ops on distinct bits. Returns its size; *rot3 tells the
 // first kind.
 template <typename T, int A>
-__device__ __forceinline__ int group_at(const MicroOp *ops, int o, int nops, bool *rot3) {
+__device__ __forceinline__ int group_at(const OpHead *ops, int o, int nops, bool *rot3) {
     constexpr int kMaxGroup = sizeof(T) == 8 && A != AR_FMA ? 2 : 3;
     *rot3 = false;
     if (kMaxGroup == 2 && o + 2 < nops && ops[o].kind == MOP_RT && ops[o + 1].kind == MOP_RT &&
@@ -110,14 +122,14 @@ __device__ __forceinline__ int group_at(const MicroOp *ops, int o, int nops, boo
 }
 
 template <typename R>
-__device__ __forceinline__ uint32_t jgather(const MicroOp &op, uint32_t jo, uint32_t v) {
+__device__ __forceinline__ uint32_t jgather(const OpHead &op, uint32_t jo, uint32_t v) {
     uint32_t j = jo;
     for (uint32_t b = 0; b < op.k; b++)
         if (!(op.loc[b] & kOuterFlag)) j |= ((v >> op.loc[b]) & 1) << b;
     return j;
 }
 
-__device__ __forceinline__ uint32_t jouter(const MicroOp &op, uint64_t base) {
+__device__ __forceinline__ uint32_t jouter(const OpHead &op, uint64_t base) {
     uint32_t jo = 0;
     for (uint32_t b = 0; b < op.k; b++)
         if (op.loc[b] & kOuterFlag) jo |= (uint32_t)((base >> (op.loc[b] & ~kOuterFlag)) & 1) << b;
@@ -129,13 +141,10 @@ __device__ __forceinline__ uint32_t jouter(const MicroOp &op, uint64_t base) {
 // elements: each gate updates the same pairs with the same arithmetic, in the
 // same order, as one op at a time. The pair swaps of flipped RT ops commute
 // with the group's other gates (other bits), so they all happen at the store:
-// element e goes to the slot of e ^ flips. With FUSE_DK the table diagonal
-// `dk` (the op just before the group, double-float tables) scales each
-// element first, exactly as its own pass would.
-template <typename T, int A, typename R, int G, bool ROT_ONLY = false, bool FUSE_DK = false>
-__device__ void apply_u1_group(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *coef, int o, uint32_t size,
-                               uint32_t *bad, const MicroOp *dk = nullptr, const char *tables = nullptr,
-                               uint64_t base = 0) {
+// element e goes to the slot of e ^ flips.
+template <typename T, int A, typename R, int G, bool ROT_ONLY = false>
+__device__ void apply_u1_group(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *coef, int o, uint32_t size,
+                               uint32_t *bad) {
     constexpr int E = 1 << G;
     uint32_t bits[G], sorted[G];
 #pragma unroll
@@ -149,10 +158,10 @@ __device__ void apply_u1_group(R *sr, R *si, const MicroOp *ops, const OpCoef<T,
                 sorted[j] = sorted[j - 1];
                 sorted[j - 1] = x;
             }
-    uint32_t flips = 0, bad_bit = 0;
+    uint32_t fmask = 0, bad_bit = 0;
 #pragma unroll
     for (int g = 0; g < G; g++) {
-        if (ops[o + g].kind == MOP_RT && ops[o + g].b) flips |= 1u << g;
+        if (ops[o + g].kind == MOP_RT && ops[o + g].b) fmask |= 1u << bits[g];
         if ((1u << bits[g]) >= size) bad_bit = bits[g];
     }
     // every slot is inside the tile when the bits are (v < size / 2^G with
@@ -162,33 +171,15 @@ __device__ void apply_u1_group(R *sr, R *si, const MicroOp *ops, const OpCoef<T,
         if (threadIdx.x == 0) *bad = bad_bit | 0x80000000u;
         return;
     }
-    // flipped elements: slot(e ^ flips) = slot(e) ^ fmask
-    uint32_t fmask = 0;
-#pragma unroll
-    for (int g = 0; g < G; g++) fmask |= ((flips >> g) & 1u) << bits[g];
-    // fused diagonal: element e of the group reads table entry jb(v) ^ tp(e),
-    // jb from the support bits outside the group, tp from the group's bits
-    uint32_t jo = 0, tb[G];
-    const float4 *dtab = nullptr;
-    if constexpr (FUSE_DK) {
-        jo = jouter(*dk, base);
-        dtab = reinterpret_cast<const float4 *>(tables + dk->table);
-#pragma unroll
-        for (int g = 0; g < G; g++) {
-            tb[g] = 0;
-            for (uint32_t b = 0; b < dk->k; b++)
-                if (dk->loc[b] == bits[g]) tb[g] = 1u << b;
-        }
-    }
     for (uint32_t p = threadIdx.x; p < size / E; p += blockDim.x) {
         uint32_t v = p;
 #pragma unroll
         for (int g = 0; g < G; g++) v = ((v >> sorted[g]) << (sorted[g] + 1)) | (v & ((1u << sorted[g]) - 1));
-        // element e of the group sits at v | (bits selected by e)
+        // element e of the group sits at v ^ (bits selected by e)
         // (recomputed at the store so the indices need no registers across
-        // the arithmetic)
-        auto slot = [&](uint32_t e) {
-            uint32_t w = v;
+        // the arithmetic); flipped elements: slot(e ^ flips) = slot(e) ^ fmask
+        auto slot = [&](uint32_t base_v, uint32_t e) {
+            uint32_t w = base_v;
 #pragma unroll
             for (int g = 0; g < G; g++)
                 if ((e >> g) & 1u) w ^= 1u << bits[g];
@@ -197,25 +188,9 @@ __device__ void apply_u1_group(R *sr, R *si, const MicroOp *ops, const OpCoef<T,
         R xr[E], xi[E];
 #pragma unroll
         for (int e = 0; e < E; e++) {
-            const uint32_t w = slot(e);
+            const uint32_t w = slot(v, (uint32_t)e);
             xr[e] = sr[w];
             xi[e] = si[w];
-        }
-        if constexpr (FUSE_DK) {
-            uint32_t jb = jo;
-            for (uint32_t b = 0; b < dk->k; b++) {
-                const uint32_t l = dk->loc[b];
-                if (!(l & kOuterFlag)) jb |= ((v >> l) & 1u) << b;
-            }
-#pragma unroll
-            for (int e = 0; e < E; e++) {
-                uint32_t j = jb;
-#pragma unroll
-                for (int g = 0; g < G; g++)
-                    if ((e >> g) & 1) j ^= tb[g];
-                const float4 w = __ldg(dtab + j);
-                cscale_df(make_float2(w.x, w.y), make_float2(w.z, w.w), xr[e], xi[e]);
-            }
         }
 #pragma unroll
         for (int g = 0; g < G; g++) {
@@ -258,36 +233,311 @@ __device__ void apply_u1_group(R *sr, R *si, const MicroOp *ops, const OpCoef<T,
                         pair_update<T, A == AR_EXACT>(m, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
             }
         }
-        v ^= fmask;
+        const uint32_t vs = v ^ fmask;
 #pragma unroll
         for (int e = 0; e < E; e++) {
-            const uint32_t w = slot((uint32_t)e);
+            const uint32_t w = slot(vs, (uint32_t)e);
             sr[w] = xr[e];
             si[w] = xi[e];
         }
     }
 }
 
-// Apply the sweep's micro-ops to one tile. For A == AR_DF the tile's f64
-// slots hold (hi, lo) float pairs (R = float2); otherwise R = T.
+// ------------------------------------------------------------------
+// Register passes of double-float sweeps, resolved once per job.
+//
+// A pass is a register group (one to three one-qubit ops on distinct tile
+// bits, as group_at forms them) together with the table diagonal right
+// before it and, before that, a block of CX ops whose targets are all group
+// bits. The diagonal scales each element before the gates, exactly as its
+// own pass would. A CX moves data only within a group whose bits hold its
+// target, so the CX block becomes the load permutation: logical element y
+// (group coordinates; the other bits v fixed) is read from
+// pi_1(pi_2(...pi_n(y))), pi_i flipping the target where the control is
+// set. Over GF(2) that is y -> M y + sum_i ctl_i(v) w_i: controls among the
+// group bits make M, controls outside them (local bits of v, or outer qubits
+// fixed per tile) add the translations w_i. One thread derives all of it in
+// load_job; per tile a pass reads a few shared words.
+struct GroupInfo {
+    uint8_t G, rot3, skip, first;  // G = 0: no pass starts at this op
+    uint8_t nloc, nout, ntr, has_dk;
+    uint8_t sorted[3];             // group bits ascending (zero insertion)
+    uint8_t tb[3];                 // table bit of each group coordinate (0xff: not in the support)
+    uint8_t loc[8], locb[8];       // support bits outside the group -> table bit
+    uint8_t outq[8], outb[8];      // outer support qubits -> table bit
+    uint8_t trc[4];                // translation controls: local bit, or 0x80 | outer qubit
+    uint16_t gm[3];                // slot pattern of group coordinate g (1 << bit)
+    uint16_t pm[3];                // load pattern of coordinate g (column g of M, as slots)
+    uint16_t trw[4];               // translation patterns
+    uint16_t fmask;                // store pattern of the flipped coordinates
+    uint32_t tab_off;
+};
+
+// One thread: walk the ops the way apply_ops will and describe each pass.
+template <typename T, int A>
+__device__ void plan_passes(const OpHead *ops, int nops, uint32_t tile_log2, bool fold, GroupInfo *gi,
+                            uint32_t *bad) {
+    for (int i = 0; i < nops; i++) gi[i].G = 0;
+    int o = 0;
+    while (o < nops) {
+        const OpHead &op = ops[o];
+        int first = -1, jdk = -1, cx0 = -1, ncx = 0;
+        if (fold && op.kind == MOP_CX) {
+            int j = o;
+            bool ok = true;
+            while (j < nops && ops[j].kind == MOP_CX && j - o < kMaxFoldCx) {
+                ok &= !(ops[j].b & kOuterFlag);
+                j++;
+            }
+            const bool dk = j < nops && ops[j].kind == MOP_DK && ops[j].k <= 8;
+            const int g0 = dk ? j + 1 : j;
+            if (ok && g0 < nops && is_1q(ops[g0].kind)) {
+                bool rot3;
+                const int g = group_at<T, A>(ops, g0, nops, &rot3);
+                for (int i = o; i < j; i++) {
+                    bool hit = false;
+                    for (int h = 0; h < g; h++) hit |= ops[g0 + h].a == ops[i].b;
+                    ok &= hit;
+                }
+                if (ok) {
+                    first = g0;
+                    jdk = dk ? j : -1;
+                    cx0 = o;
+                    ncx = j - o;
+                }
+            }
+        } else if (op.kind == MOP_DK && op.k <= 8 && o + 1 < nops && is_1q(ops[o + 1].kind)) {
+            first = o + 1;
+            jdk = o;
+        } else if (is_1q(op.kind)) {
+            first = o;
+        }
+        if (first < 0) {
+            o++;
+            continue;
+        }
+        bool rot3;
+        const int G = group_at<T, A>(ops, first, nops, &rot3);
+        GroupInfo &q = gi[o];
+        uint32_t bits[3] = {0, 0, 0};
+        bool in_tile = true;
+        for (int g = 0; g < G; g++) {
+            bits[g] = ops[first + g].a;
+            in_tile &= bits[g] < tile_log2;
+        }
+        if (!in_tile) {  // cannot happen for a planned sweep: recorded, ops run one by one
+            *bad = 0x80000000u | (uint32_t)o;
+            o++;
+            continue;
+        }
+        q.G = (uint8_t)G;
+        q.rot3 = rot3;
+        q.first = (uint8_t)first;
+        q.skip = (uint8_t)(first + G - o);
+        q.fmask = 0;
+        for (int g = 0; g < G; g++) {
+            q.gm[g] = q.pm[g] = (uint16_t)(1u << bits[g]);
+            if (ops[first + g].kind == MOP_RT && ops[first + g].b) q.fmask |= (uint16_t)(1u << bits[g]);
+        }
+        uint32_t srt[3] = {bits[0], bits[1], bits[2]};
+        for (int a = 1; a < G; a++)
+            for (int b = a; b > 0 && srt[b] < srt[b - 1]; b--) {
+                const uint32_t x = srt[b];
+                srt[b] = srt[b - 1];
+                srt[b - 1] = x;
+            }
+        for (int g = 0; g < 3; g++) q.sorted[g] = (uint8_t)srt[g];
+        q.has_dk = jdk >= 0;
+        q.nloc = q.nout = 0;
+        for (int g = 0; g < 3; g++) q.tb[g] = 0xff;
+        if (jdk >= 0) {
+            const OpHead &d = ops[jdk];
+            q.tab_off = (uint32_t)d.table;
+            for (uint32_t b = 0; b < d.k; b++) {
+                const uint32_t l = d.loc[b];
+                if (l & kOuterFlag) {
+                    q.outq[q.nout] = (uint8_t)(l & ~kOuterFlag);
+                    q.outb[q.nout++] = (uint8_t)b;
+                    continue;
+                }
+                int hit = -1;
+                for (int g = 0; g < G; g++)
+                    if (bits[g] == l) hit = g;
+                if (hit >= 0) {
+                    q.tb[hit] = (uint8_t)b;
+                } else {
+                    q.loc[q.nloc] = (uint8_t)l;
+                    q.locb[q.nloc++] = (uint8_t)b;
+                }
+            }
+        }
+        // CX block as an affine map over the group coordinates, composed
+        // from the last CX (applied to y first) to the first
+        q.ntr = 0;
+        if (ncx > 0) {
+            uint32_t col[3] = {1u, 2u, 4u}, trv[kMaxFoldCx];
+            uint8_t trc[kMaxFoldCx];
+            int ntr = 0;
+            for (int i = ncx - 1; i >= 0; i--) {
+                const OpHead &x = ops[cx0 + i];
+                int tau = 0, kap = -1;
+                for (int g = 0; g < G; g++) {
+                    if (bits[g] == x.b) tau = g;
+                    if (!(x.a & kOuterFlag) && bits[g] == x.a) kap = g;
+                }
+                if (kap >= 0) {  // y_tau ^= y_kap
+                    for (int g = 0; g < G; g++)
+                        if ((col[g] >> kap) & 1u) col[g] ^= 1u << tau;
+                    for (int t = 0; t < ntr; t++)
+                        if ((trv[t] >> kap) & 1u) trv[t] ^= 1u << tau;
+                } else {  // y_tau ^= (control outside the group)
+                    trc[ntr] = x.a & kOuterFlag ? (uint8_t)(0x80u | (x.a & ~kOuterFlag)) : (uint8_t)x.a;
+                    trv[ntr++] = 1u << tau;
+                }
+            }
+            auto pattern = [&](uint32_t y) {
+                uint32_t w = 0;
+                for (int g = 0; g < G; g++)
+                    if ((y >> g) & 1u) w |= 1u << bits[g];
+                return (uint16_t)w;
+            };
+            for (int g = 0; g < G; g++) q.pm[g] = pattern(col[g]);
+            q.ntr = (uint8_t)ntr;
+            for (int t = 0; t < ntr; t++) {
+                q.trc[t] = trc[t];
+                q.trw[t] = pattern(trv[t]);
+            }
+        }
+        o += q.skip;
+    }
+}
+
+// One pass (see GroupInfo) of a double-float sweep. The descriptor's fields
+// are read from shared memory where they are used, which keeps the 80-register
+// budget for the group's amplitudes.
+template <typename T, int A, int G, bool ROT_ONLY, bool HAS_DK, bool HAS_CX>
+__device__ void run_pass(const GroupInfo &gi, float2 *sr, float2 *si, const OpHead *ops, const OpCoef<T, A> *coef,
+                         uint32_t size, const char *tables, uint64_t base) {
+    constexpr int E = 1 << G;
+    const int o = gi.first;
+    uint32_t jo = 0, u0 = 0;
+    if constexpr (HAS_DK) {
+        for (int i = 0; i < gi.nout; i++) jo |= (uint32_t)((base >> gi.outq[i]) & 1u) << gi.outb[i];
+    }
+    if constexpr (HAS_CX) {
+        for (int t = 0; t < gi.ntr; t++)
+            if ((gi.trc[t] & 0x80u) && ((base >> (gi.trc[t] & 0x7fu)) & 1u)) u0 ^= gi.trw[t];
+    }
+    for (uint32_t p = threadIdx.x; p < size / E; p += blockDim.x) {
+        uint32_t v = p;
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            const uint32_t s = gi.sorted[g];
+            v = ((v >> s) << (s + 1)) | (v & ((1u << s) - 1));
+        }
+        float2 xr[E], xi[E];
+        {
+            uint32_t lv = v;
+            if constexpr (HAS_CX) {
+                lv ^= u0;
+                for (int t = 0; t < gi.ntr; t++)
+                    if (!(gi.trc[t] & 0x80u) && ((v >> gi.trc[t]) & 1u)) lv ^= gi.trw[t];
+            }
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+                uint32_t w = lv;
+#pragma unroll
+                for (int g = 0; g < G; g++)
+                    if ((e >> g) & 1) w ^= HAS_CX ? gi.pm[g] : gi.gm[g];
+                xr[e] = sr[w];
+                xi[e] = si[w];
+            }
+        }
+        if constexpr (HAS_DK) {
+            const float4 *dtab = reinterpret_cast<const float4 *>(tables + gi.tab_off);
+            uint32_t jb = jo;
+            for (int i = 0; i < gi.nloc; i++) jb |= ((v >> gi.loc[i]) & 1u) << gi.locb[i];
+#pragma unroll
+            for (int e = 0; e < E; e++) {
+                uint32_t j = jb;
+#pragma unroll
+                for (int g = 0; g < G; g++)
+                    if (((e >> g) & 1) && gi.tb[g] != 0xff) j ^= 1u << gi.tb[g];
+                const float4 w = __ldg(dtab + j);
+                cscale_df(make_float2(w.x, w.y), make_float2(w.z, w.w), xr[e], xi[e]);
+            }
+        }
+#pragma unroll
+        for (int g = 0; g < G; g++) {
+            if (ROT_ONLY || ops[o + g].kind == MOP_RT) {
+                const float2 t = coef[o + g].v[0];
+#pragma unroll
+                for (int e = 0; e < E; e++)
+                    if (!((e >> g) & 1)) pair_update_rot_df(t, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+            } else if (ops[o + g].kind == MOP_R1) {
+                float2 r[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) r[i] = coef[o + g].v[i];
+#pragma unroll
+                for (int e = 0; e < E; e++)
+                    if (!((e >> g) & 1)) pair_update_rdf(r, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+            } else {
+                MatDF m;
+#pragma unroll
+                for (int i = 0; i < 8; i++) m.v[i] = coef[o + g].v[i];
+#pragma unroll
+                for (int e = 0; e < E; e++)
+                    if (!((e >> g) & 1)) pair_update_df(m, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+            }
+        }
+        const uint32_t vs = v ^ gi.fmask;
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            uint32_t w = vs;
+#pragma unroll
+            for (int g = 0; g < G; g++)
+                if ((e >> g) & 1) w ^= gi.gm[g];
+            sr[w] = xr[e];
+            si[w] = xi[e];
+        }
+    }
+}
+
+template <typename T, int A, int G, bool ROT_ONLY>
+__device__ void run_pass_any(const GroupInfo &gi, float2 *sr, float2 *si, const OpHead *ops,
+                             const OpCoef<T, A> *coef, uint32_t size, const char *tables, uint64_t base) {
+    if (gi.has_dk) {
+        if (gi.ntr || gi.pm[0] != gi.gm[0] || (G > 1 && gi.pm[G - 1] != gi.gm[G - 1]) ||
+            (G > 2 && gi.pm[1] != gi.gm[1]))
+            run_pass<T, A, G, ROT_ONLY, true, true>(gi, sr, si, ops, coef, size, tables, base);
+        else
+            run_pass<T, A, G, ROT_ONLY, true, false>(gi, sr, si, ops, coef, size, tables, base);
+    } else {
+        if (gi.ntr || gi.pm[0] != gi.gm[0] || (G > 1 && gi.pm[G - 1] != gi.gm[G - 1]) ||
+            (G > 2 && gi.pm[1] != gi.gm[1]))
+            run_pass<T, A, G, ROT_ONLY, false, true>(gi, sr, si, ops, coef, size, tables, base);
+        else
+            run_pass<T, A, G, ROT_ONLY, false, false>(gi, sr, si, ops, coef, size, tables, base);
+    }
+}
+
+// gis: the job's register passes (double-float sweeps; see GroupInfo).
 template <typename T, int A, typename R>
-__device__ void apply_ops(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *coef, int nops, uint64_t base,
-                          uint32_t size, const char *tables, uint32_t *bad, uint16_t *jlut) {
+__device__ void apply_ops(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *coef, int nops, uint64_t base,
+                          uint32_t size, const char *tables, uint32_t *bad, uint16_t *jlut, const GroupInfo *gis) {
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int o = 0; o < nops; o++) {
-        const MicroOp &op = ops[o];
+        const OpHead &op = ops[o];
         if constexpr (A == AR_DF) {
-            // a table diagonal right before a register group rides in its pass
-            if (op.kind == MOP_DK && o + 1 < nops && is_1q(ops[o + 1].kind)) {
-                bool rot3;
-                const int g = group_at<T, A>(ops, o + 1, nops, &rot3);
-                if (rot3)
-                    apply_u1_group<T, A, R, 3, true, true>(sr, si, ops, coef, o + 1, size, bad, &op, tables, base);
-                else if (g == 2)
-                    apply_u1_group<T, A, R, 2, false, true>(sr, si, ops, coef, o + 1, size, bad, &op, tables, base);
+            const GroupInfo &gi = gis[o];
+            if (gi.G) {
+                if (gi.rot3)
+                    run_pass_any<T, A, 3, true>(gi, sr, si, ops, coef, size, tables, base);
+                else if (gi.G == 2)
+                    run_pass_any<T, A, 2, false>(gi, sr, si, ops, coef, size, tables, base);
                 else
-                    apply_u1_group<T, A, R, 1, false, true>(sr, si, ops, coef, o + 1, size, bad, &op, tables, base);
-                o += g;
+                    run_pass_any<T, A, 1, false>(gi, sr, si, ops, coef, size, tables, base);
+                o += gi.skip - 1;
                 __syncthreads();
                 continue;
             }
@@ -441,7 +691,7 @@ __device__ void apply_ops(R *sr, R *si, const MicroOp *ops, const OpCoef<T, A> *
 template <typename T, int A>
 struct SweepSmem {
     uint64_t bar;
-    MicroOp ops[kMaxMicroOps];
+    OpHead ops[kMaxMicroOps];
     OpCoef<T, A> coef[kMaxMicroOps];
     uint32_t hpos[16];     // tile bit L + j holds qubit hpos[j] (any order)
     uint32_t hsorted[16];  // the same qubits ascending (tile base)
@@ -452,16 +702,19 @@ struct SweepSmem {
     int fail;
     uint32_t fail_tile, done_tiles, bad;
     uint16_t jlut[256 + kJlutHigh];  // diagonal index tables of the current DK op
+    GroupInfo gi[kMaxMicroOps];      // register passes (double-float sweeps)
 };
 
 // All threads: make (gops, nops, L, H, hpos) the CTA's current job.
 template <typename T, int A>
 __device__ void load_job(SweepSmem<T, A> &c, const MicroOp *gops, int nops, uint32_t L, uint32_t H,
-                         const uint32_t *hpos) {
+                         const uint32_t *hpos, bool fold) {
     const int tid = threadIdx.x;
     __syncthreads();  // the previous job's tiles are done with the tables
-    for (int i = tid; i < nops * (int)(sizeof(MicroOp) / 4); i += blockDim.x)
-        reinterpret_cast<uint32_t *>(c.ops)[i] = reinterpret_cast<const uint32_t *>(gops)[i];
+    constexpr int kHeadWords = (int)(sizeof(OpHead) / 4), kOpWords = (int)(sizeof(MicroOp) / 4);
+    for (int i = tid; i < nops * kHeadWords; i += blockDim.x)
+        reinterpret_cast<uint32_t *>(c.ops)[i] =
+            reinterpret_cast<const uint32_t *>(gops)[(i / kHeadWords) * kOpWords + i % kHeadWords];
     if (tid < 16) c.hpos[tid] = tid < (int)H ? hpos[tid] : 0u;
     if (tid == 0) {
         for (uint32_t j = 0; j < H; j++) {  // insertion sort, H <= 7
@@ -482,7 +735,7 @@ __device__ void load_job(SweepSmem<T, A> &c, const MicroOp *gops, int nops, uint
     }
     __syncthreads();
     if (tid < nops) {
-        const MicroOp &op = c.ops[tid];
+        const MicroOp &op = gops[tid];  // matrix entries from global memory
         if (op.kind == MOP_U1 || op.kind == MOP_D1 || op.kind == MOP_R1 || op.kind == MOP_RT) {
             const int cnt = op.kind == MOP_U1 ? 8 : op.kind == MOP_RT ? 1 : 4;
             for (int i = 0; i < cnt; i++) {
@@ -498,6 +751,7 @@ __device__ void load_job(SweepSmem<T, A> &c, const MicroOp *gops, int nops, uint
         for (int o = 0; o < nops; o++)
             ar |= c.ops[o].kind != MOP_CX && c.ops[o].kind != MOP_SWAP;
         c.has_arith = ar;
+        if constexpr (A == AR_DF) plan_passes<T, A>(c.ops, nops, L + H, fold, c.gi, &c.bad);
     }
     __syncthreads();
 }
@@ -538,7 +792,7 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
             }
             __syncthreads();
         }
-        apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut);
+        apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut, c.gi);
         if (c.has_arith) {
             for (uint32_t v = tid; v < size; v += blockDim.x) {
                 dr[v] = df_to_f64(fr[v]);
@@ -546,7 +800,7 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
             }
         }
     } else {
-        apply_ops<T, A, T>(sre, sim, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut);
+        apply_ops<T, A, T>(sre, sim, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut, c.gi);
     }
     fence_async_smem();
     __syncthreads();
@@ -613,7 +867,7 @@ __global__ void __launch_bounds__(kSweepThreads, kSweepCtasPerSm)
     T *sre = reinterpret_cast<T *>(smem);
     T *sim = sre + (1u << (g.L + g.H));
     sweep_init(c);
-    load_job(c, gops, nops, g.L, g.H, g.hpos);
+    load_job(c, gops, nops, g.L, g.H, g.hpos, true);
     uint32_t phase = 0;
     for (uint64_t t = blockIdx.x; t < g.ntiles; t += gridDim.x)
         if (!process_tile(c, re, im, t, tables, sre, sim, phase)) break;
@@ -648,7 +902,9 @@ __global__ void __launch_bounds__(kSweepThreads, kSweepCtasPerSm)
                 else hi = mid;
             }
             const SweepJob &Jn = jobs[lo];
-            load_job(c, reinterpret_cast<const MicroOp *>(blob + Jn.ops_off), (int)Jn.nops, Jn.L, Jn.H, Jn.hpos);
+            // CX folding stays off here: the packed kernel's extra live state spills
+            load_job(c, reinterpret_cast<const MicroOp *>(blob + Jn.ops_off), (int)Jn.nops, Jn.L, Jn.H, Jn.hpos,
+                     false);
             cur = (int)lo;
             job_lo = Jn.tile_start;
             job_hi = Jn.tile_start + Jn.ntiles;

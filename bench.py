@@ -41,12 +41,15 @@ SWEEP_DF_PIPES = {"issue_active_pct": 73.0, "fma_pipe_pct": 58.0, "fp64_pipe_pct
 # FP32 instructions per amplitude of each double-float sweep micro-op
 # (zeno_gb300/csrc/zc_arith.cuh): a product is 4 (FMUL + 3 FFMA), TwoSum 6,
 # renormalisation 3. Complex 2x2: four 4-term dot products per pair
-# (4*4 + 3*6 + 6 + 3 = 43 each) = 86; real 2x2 and diagonals: 2-term dot
-# products (2*4 + 6 + 2 + 3 = 19), two per amplitude = 38; rotation
-# [[1, -t], [t, 1]]: x + t*y (4 + 6 + 2 + 3 = 15), two per amplitude = 30.
-# CX and SWAP move data only.
-DF_FP32_INSTR_PER_AMP = {"complex": 86, "diag1": 38, "diag_table": 38, "cx": 0, "swap": 0, "real": 38,
-                         "rotation": 30}
+# (4*4 + 3*6 + 6 + 3 = 43 each) = 86; real 2x2 and one-qubit diagonals:
+# 2-term dot products (2*4 + 6 + 2 + 3 = 19), two per amplitude = 38. Inside
+# a register pass the table diagonal and the rotations chain unnormalised
+# pairs: table diagonal 2 x (2*4 + 6 + 2) = 32, rotation [[1, -t], [t, 1]]
+# 2 x (4 + 6 + 2) = 24, plus the pass's one renormalisation (2 x 3 per
+# amplitude) shared by its (usually three) rotations: 26. CX and SWAP move
+# data only.
+DF_FP32_INSTR_PER_AMP = {"complex": 86, "diag1": 38, "diag_table": 32, "cx": 0, "swap": 0, "real": 38,
+                         "rotation": 26}
 FP32_INSTR_PEAK = 34.3e12  # measured FMA issue rate (zeno_gb300/probes/fp_peaks.cu)
 
 

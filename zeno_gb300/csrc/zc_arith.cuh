@@ -265,6 +265,47 @@ __device__ __forceinline__ float2 df_axpy(float2 x, float2 t, float2 y) {
     return df_norm(s, __fadd_rn(x.y, __fadd_rn(e, r)));
 }
 
+// Unnormalised variants for chains of operations inside one register pass:
+// the (s, lo) pair is left as TwoSum and the error terms give it (|lo| a few
+// ulps of s at most); products and TwoSums of the next operation stay exact in
+// their hi parts whatever the pair's normalisation, so the chain keeps the
+// double-float error bound relative to its inputs. df_norm once at the end.
+__device__ __forceinline__ float2 df_axpy_u(float2 x, float2 t, float2 y) {
+    float p, e, r;
+    df_prod(t, y, p, e);
+    const float s = two_sum(x.x, p, r);
+    return make_float2(s, __fadd_rn(x.y, __fadd_rn(e, r)));
+}
+
+__device__ __forceinline__ float2 df_dot2_u(float2 x0, float2 y0, float2 x1, float2 y1) {
+    float p0, e0, p1, e1, r1;
+    df_prod(x0, y0, p0, e0);
+    df_prod(x1, y1, p1, e1);
+    const float s = two_sum(p0, p1, r1);
+    return make_float2(s, __fadd_rn(r1, __fadd_rn(e0, e1)));
+}
+
+__device__ __forceinline__ float2 df_renorm(float2 v) { return df_norm(v.x, v.y); }
+
+__device__ __forceinline__ void pair_update_rot_df_u(float2 t, float2 &ar, float2 &ai, float2 &br, float2 &bi) {
+    const float2 nt = df_neg(t);
+    const float2 nar = df_axpy_u(ar, nt, br);
+    const float2 nai = df_axpy_u(ai, nt, bi);
+    const float2 nbr = df_axpy_u(br, t, ar);
+    const float2 nbi = df_axpy_u(bi, t, ai);
+    ar = nar;
+    ai = nai;
+    br = nbr;
+    bi = nbi;
+}
+
+__device__ __forceinline__ void cscale_df_u(float2 wr, float2 wi, float2 &ar, float2 &ai) {
+    const float2 nr = df_dot2_u(wr, ar, df_neg(wi), ai);
+    const float2 ni = df_dot2_u(wr, ai, wi, ar);
+    ar = nr;
+    ai = ni;
+}
+
 // Rotation update of (a, b) with unit diagonal: [[1, -t], [t, 1]]
 // (|t| <= 1; the scale that makes it orthogonal lives in a diagonal).
 __device__ __forceinline__ void pair_update_rot_df(float2 t, float2 &ar, float2 &ai, float2 &br, float2 &bi) {

@@ -464,16 +464,18 @@ __device__ void run_pass(const GroupInfo &gi, float2 *sr, float2 *si, const OpHe
                 for (int g = 0; g < G; g++)
                     if (((e >> g) & 1) && gi.tb[g] != 0xff) j ^= 1u << gi.tb[g];
                 const float4 w = __ldg(dtab + j);
-                cscale_df(make_float2(w.x, w.y), make_float2(w.z, w.w), xr[e], xi[e]);
+                cscale_df_u(make_float2(w.x, w.y), make_float2(w.z, w.w), xr[e], xi[e]);
             }
         }
+        // the diagonal and the rotations chain unnormalised pairs (every
+        // double-float op here accepts them); renormalised once at the store
 #pragma unroll
         for (int g = 0; g < G; g++) {
             if (ROT_ONLY || ops[o + g].kind == MOP_RT) {
                 const float2 t = coef[o + g].v[0];
 #pragma unroll
                 for (int e = 0; e < E; e++)
-                    if (!((e >> g) & 1)) pair_update_rot_df(t, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                    if (!((e >> g) & 1)) pair_update_rot_df_u(t, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
             } else if (ops[o + g].kind == MOP_R1) {
                 float2 r[4];
 #pragma unroll
@@ -497,8 +499,8 @@ __device__ void run_pass(const GroupInfo &gi, float2 *sr, float2 *si, const OpHe
 #pragma unroll
             for (int g = 0; g < G; g++)
                 if ((e >> g) & 1) w ^= gi.gm[g];
-            sr[w] = xr[e];
-            si[w] = xi[e];
+            sr[w] = df_renorm(xr[e]);
+            si[w] = df_renorm(xi[e]);
         }
     }
 }

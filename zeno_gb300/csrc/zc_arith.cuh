@@ -100,10 +100,10 @@ __device__ __forceinline__ void cmac(T wr, T wi, T xr, T xi, T &ar, T &ai) {
 // mode keeps the state in f64 in HBM but does the gate arithmetic on the
 // FP32 pipe with unevaluated (hi, lo) float pairs (Dekker 1971; error-free
 // TwoSum of Knuth, two-product via FMA). Conversions between f64 and the
-// pair use integer bit operations only, never the FP64 pipe. A gate costs
-// about 43 FP32 operations per output component and carries ~2^-46
-// relative error; the f64 <-> pair round trip truncates at 2^-47 and
-// 2^-52. Zero, subnormals and |x| < 2^-126 map to 0.
+// pair use integer and FP32 operations only, never the FP64 pipe. A general
+// gate costs about 43 FP32 operations per output component and carries
+// ~2^-46 relative error; f64 -> pair truncates at 2^-47, pair -> f64 rounds
+// to nearest. Zero, subnormals and |x| < 2^-126 map to 0.
 
 // f64 -> (hi, lo): hi = x truncated to 24 bits, lo = the next 23 bits.
 __device__ __forceinline__ float2 df_from_f64(double x) {
@@ -146,31 +146,24 @@ __device__ __forceinline__ double f32_to_f64_exact(float x) {
 __device__ __forceinline__ double widen(double x) { return x; }
 __device__ __forceinline__ double widen(float x) { return f32_to_f64_exact(x); }
 
-// (hi, lo) -> f64 with |lo| <= ulp(hi): 53-bit integer sum, truncated.
+// (hi, lo) -> f64 for |lo| <= ulp(hi): the f64 bit pattern of hi plus lo
+// counted in f64 ulps of hi's binade (|lo| <= 2^28 of them; one binade lower
+// when hi is a power of two and lo points down, where the ulp halves), scaled
+// by a power of two and rounded to an integer: the f64 nearest hi + lo.
+// |hi| < 2^-75 keeps hi alone; zero and subnormal hi give 0.
 __device__ __forceinline__ double df_to_f64(float2 v) {
-    const unsigned hb = __float_as_uint(v.x);
-    const int eh = (int)((hb >> 23) & 0xff);
-    if (eh == 0) return 0.0;
-    const unsigned long long sh = hb & 0x80000000u;
-    unsigned long long M = (unsigned long long)((hb & 0x7fffffu) | 0x800000u) << 29;
-    const unsigned lb = __float_as_uint(v.y);
-    const int el = (int)((lb >> 23) & 0xff);
-    if (el != 0) {
-        const unsigned long long ml = (lb & 0x7fffffu) | 0x800000u;
-        const int d = el - eh + 29;
-        const unsigned long long L = d >= 0 ? (ml << (d > 10 ? 10 : d)) : (d > -40 ? (ml >> -d) : 0ull);
-        if ((lb & 0x80000000u) == (unsigned)sh) M += L;
-        else M -= L;
-    }
-    int E = eh + 896;
-    if (M >> 53) {
-        M >>= 1;
-        E += 1;
-    } else if (!(M >> 52)) {
-        M <<= 1;
-        E -= 1;
-    }
-    return __longlong_as_double((long long)((sh << 32) | ((unsigned long long)E << 52) | (M & 0xfffffffffffffull)));
+    const unsigned hb = __float_as_uint(v.x), lb = __float_as_uint(v.y);
+    const unsigned eh = (hb >> 23) & 0xffu;
+    if (eh == 0u) return 0.0;
+    const unsigned mant = hb & 0x7fffffu;
+    const unsigned long long hbits =
+        ((unsigned long long)((hb & 0x80000000u) | ((eh + 896u) << 20) | (mant >> 3)) << 32) |
+        (unsigned long long)(mant << 29);
+    const bool down = mant == 0u && ((hb ^ lb) & 0x80000000u) && (lb & 0x7fffffffu);
+    const unsigned se = 306u - eh + (down ? 1u : 0u);  // f32 exponent field of 2^(179 - eh (+1))
+    if (se >= 255u) return __longlong_as_double((long long)hbits);
+    const int L = __float2int_rn(__fmul_rn(v.y, __uint_as_float(se << 23)));
+    return __longlong_as_double((long long)(hbits + (unsigned long long)(long long)((hb >> 31) ? -L : L)));
 }
 
 // Exact product split: a*b = p + e with e from one FMA, plus cross terms.

@@ -274,10 +274,13 @@ struct GroupInfo {
 };
 
 // One thread: walk the ops the way apply_ops will and describe each pass.
+// *fuse_in / *fuse_out: the job starts / ends with a pass, which then also
+// converts the tile between f64 and double-float in registers.
 template <typename T, int A>
 __device__ void plan_passes(const OpHead *ops, int nops, uint32_t tile_log2, bool fold, GroupInfo *gi,
-                            uint32_t *bad) {
+                            uint32_t *bad, int *fuse_in, int *fuse_out) {
     for (int i = 0; i < nops; i++) gi[i].G = 0;
+    *fuse_out = 0;
     int o = 0;
     while (o < nops) {
         const OpHead &op = ops[o];
@@ -409,15 +412,19 @@ __device__ void plan_passes(const OpHead *ops, int nops, uint32_t tile_log2, boo
             }
         }
         o += q.skip;
+        *fuse_out = o == nops;
     }
+    *fuse_in = nops > 0 && gi[0].G != 0;
 }
 
 // One pass (see GroupInfo) of a double-float sweep. The descriptor's fields
 // are read from shared memory where they are used, which keeps the 80-register
 // budget for the group's amplitudes.
+// in_f64 / out_f64: the slots hold f64 on entry / must hold f64 on exit (the
+// sweep's first / last pass does the tile's conversion in registers).
 template <typename T, int A, int G, bool ROT_ONLY, bool HAS_DK, bool HAS_CX>
 __device__ void run_pass(const GroupInfo &gi, float2 *sr, float2 *si, const OpHead *ops, const OpCoef<T, A> *coef,
-                         uint32_t size, const char *tables, uint64_t base) {
+                         uint32_t size, const char *tables, uint64_t base, bool in_f64, bool out_f64) {
     constexpr int E = 1 << G;
     const int o = gi.first;
     uint32_t jo = 0, u0 = 0;
@@ -449,8 +456,13 @@ __device__ void run_pass(const GroupInfo &gi, float2 *sr, float2 *si, const OpHe
 #pragma unroll
                 for (int g = 0; g < G; g++)
                     if ((e >> g) & 1) w ^= HAS_CX ? gi.pm[g] : gi.gm[g];
-                xr[e] = sr[w];
-                xi[e] = si[w];
+                if (in_f64) {
+                    xr[e] = df_from_f64(reinterpret_cast<const double *>(sr)[w]);
+                    xi[e] = df_from_f64(reinterpret_cast<const double *>(si)[w]);
+                } else {
+                    xr[e] = sr[w];
+                    xi[e] = si[w];
+                }
             }
         }
         if constexpr (HAS_DK) {
@@ -499,46 +511,51 @@ __device__ void run_pass(const GroupInfo &gi, float2 *sr, float2 *si, const OpHe
 #pragma unroll
             for (int g = 0; g < G; g++)
                 if ((e >> g) & 1) w ^= gi.gm[g];
-            sr[w] = df_renorm(xr[e]);
-            si[w] = df_renorm(xi[e]);
+            if (out_f64) {
+                reinterpret_cast<double *>(sr)[w] = df_to_f64(df_renorm(xr[e]));
+                reinterpret_cast<double *>(si)[w] = df_to_f64(df_renorm(xi[e]));
+            } else {
+                sr[w] = df_renorm(xr[e]);
+                si[w] = df_renorm(xi[e]);
+            }
         }
     }
 }
 
 template <typename T, int A, int G, bool ROT_ONLY>
 __device__ void run_pass_any(const GroupInfo &gi, float2 *sr, float2 *si, const OpHead *ops,
-                             const OpCoef<T, A> *coef, uint32_t size, const char *tables, uint64_t base) {
+                             const OpCoef<T, A> *coef, uint32_t size, const char *tables, uint64_t base, bool in_f64,
+                             bool out_f64) {
+    const bool cx = gi.ntr || gi.pm[0] != gi.gm[0] || (G > 1 && gi.pm[G - 1] != gi.gm[G - 1]) ||
+                    (G > 2 && gi.pm[1] != gi.gm[1]);
     if (gi.has_dk) {
-        if (gi.ntr || gi.pm[0] != gi.gm[0] || (G > 1 && gi.pm[G - 1] != gi.gm[G - 1]) ||
-            (G > 2 && gi.pm[1] != gi.gm[1]))
-            run_pass<T, A, G, ROT_ONLY, true, true>(gi, sr, si, ops, coef, size, tables, base);
-        else
-            run_pass<T, A, G, ROT_ONLY, true, false>(gi, sr, si, ops, coef, size, tables, base);
+        if (cx) run_pass<T, A, G, ROT_ONLY, true, true>(gi, sr, si, ops, coef, size, tables, base, in_f64, out_f64);
+        else run_pass<T, A, G, ROT_ONLY, true, false>(gi, sr, si, ops, coef, size, tables, base, in_f64, out_f64);
     } else {
-        if (gi.ntr || gi.pm[0] != gi.gm[0] || (G > 1 && gi.pm[G - 1] != gi.gm[G - 1]) ||
-            (G > 2 && gi.pm[1] != gi.gm[1]))
-            run_pass<T, A, G, ROT_ONLY, false, true>(gi, sr, si, ops, coef, size, tables, base);
-        else
-            run_pass<T, A, G, ROT_ONLY, false, false>(gi, sr, si, ops, coef, size, tables, base);
+        if (cx) run_pass<T, A, G, ROT_ONLY, false, true>(gi, sr, si, ops, coef, size, tables, base, in_f64, out_f64);
+        else run_pass<T, A, G, ROT_ONLY, false, false>(gi, sr, si, ops, coef, size, tables, base, in_f64, out_f64);
     }
 }
 
-// gis: the job's register passes (double-float sweeps; see GroupInfo).
+// gis: the job's register passes (double-float sweeps; see GroupInfo);
+// fuse_in / fuse_out: its first / last pass converts the tile.
 template <typename T, int A, typename R>
 __device__ void apply_ops(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *coef, int nops, uint64_t base,
-                          uint32_t size, const char *tables, uint32_t *bad, uint16_t *jlut, const GroupInfo *gis) {
+                          uint32_t size, const char *tables, uint32_t *bad, uint16_t *jlut, const GroupInfo *gis,
+                          int fuse_in = 0, int fuse_out = 0) {
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int o = 0; o < nops; o++) {
         const OpHead &op = ops[o];
         if constexpr (A == AR_DF) {
             const GroupInfo &gi = gis[o];
             if (gi.G) {
+                const bool in_f64 = o == 0 && fuse_in, out_f64 = o + gi.skip == nops && fuse_out;
                 if (gi.rot3)
-                    run_pass_any<T, A, 3, true>(gi, sr, si, ops, coef, size, tables, base);
+                    run_pass_any<T, A, 3, true>(gi, sr, si, ops, coef, size, tables, base, in_f64, out_f64);
                 else if (gi.G == 2)
-                    run_pass_any<T, A, 2, false>(gi, sr, si, ops, coef, size, tables, base);
+                    run_pass_any<T, A, 2, false>(gi, sr, si, ops, coef, size, tables, base, in_f64, out_f64);
                 else
-                    run_pass_any<T, A, 1, false>(gi, sr, si, ops, coef, size, tables, base);
+                    run_pass_any<T, A, 1, false>(gi, sr, si, ops, coef, size, tables, base, in_f64, out_f64);
                 o += gi.skip - 1;
                 __syncthreads();
                 continue;
@@ -705,6 +722,7 @@ struct SweepSmem {
     uint32_t fail_tile, done_tiles, bad;
     uint16_t jlut[256 + kJlutHigh];  // diagonal index tables of the current DK op
     GroupInfo gi[kMaxMicroOps];      // register passes (double-float sweeps)
+    int fuse_in, fuse_out;           // the first / last pass converts the tile
 };
 
 // All threads: make (gops, nops, L, H, hpos) the CTA's current job.
@@ -753,7 +771,8 @@ __device__ void load_job(SweepSmem<T, A> &c, const MicroOp *gops, int nops, uint
         for (int o = 0; o < nops; o++)
             ar |= c.ops[o].kind != MOP_CX && c.ops[o].kind != MOP_SWAP;
         c.has_arith = ar;
-        if constexpr (A == AR_DF) plan_passes<T, A>(c.ops, nops, L + H, fold, c.gi, &c.bad);
+        c.fuse_in = c.fuse_out = 0;
+        if constexpr (A == AR_DF) plan_passes<T, A>(c.ops, nops, L + H, fold, c.gi, &c.bad, &c.fuse_in, &c.fuse_out);
     }
     __syncthreads();
 }
@@ -787,15 +806,16 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
     if constexpr (A == AR_DF) {
         double *dr = reinterpret_cast<double *>(sre), *di = reinterpret_cast<double *>(sim);
         float2 *fr = reinterpret_cast<float2 *>(sre), *fi = reinterpret_cast<float2 *>(sim);
-        if (c.has_arith) {
+        if (c.has_arith && !c.fuse_in) {
             for (uint32_t v = tid; v < size; v += blockDim.x) {
                 fr[v] = df_from_f64(dr[v]);
                 fi[v] = df_from_f64(di[v]);
             }
             __syncthreads();
         }
-        apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut, c.gi);
-        if (c.has_arith) {
+        apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut, c.gi, c.fuse_in,
+                                c.fuse_out);
+        if (c.has_arith && !c.fuse_out) {
             for (uint32_t v = tid; v < size; v += blockDim.x) {
                 dr[v] = df_to_f64(fr[v]);
                 di[v] = df_to_f64(fi[v]);

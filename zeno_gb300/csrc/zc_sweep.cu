@@ -714,7 +714,6 @@ struct SweepSmem {
     OpCoef<T, A> coef[kMaxMicroOps];
     uint32_t hpos[16];     // tile bit L + j holds qubit hpos[j] (any order)
     uint32_t hsorted[16];  // the same qubits ascending (tile base)
-    uint64_t row_off[1 << kMaxSweepHigh];
     int nops;
     uint32_t L, H;
     int has_arith;
@@ -742,11 +741,6 @@ __device__ void load_job(SweepSmem<T, A> &c, const MicroOp *gops, int nops, uint
             for (; i > 0 && c.hsorted[i - 1] > x; i--) c.hsorted[i] = c.hsorted[i - 1];
             c.hsorted[i] = x;
         }
-    }
-    for (uint32_t r = tid; r < (1u << H); r += blockDim.x) {
-        uint64_t o = 0;
-        for (uint32_t j = 0; j < H; j++) o |= (uint64_t)((r >> j) & 1) << hpos[j];
-        c.row_off[r] = o;
     }
     if (tid == 0) {
         c.nops = nops;
@@ -777,6 +771,14 @@ __device__ void load_job(SweepSmem<T, A> &c, const MicroOp *gops, int nops, uint
     __syncthreads();
 }
 
+// Global offset of row r of a tile: bit j of r at qubit hpos[j].
+template <typename T, int A>
+__device__ __forceinline__ uint64_t row_offset(const SweepSmem<T, A> &c, uint32_t r) {
+    uint64_t o = 0;
+    for (uint32_t j = 0; j < c.H; j++) o |= (uint64_t)((r >> j) & 1u) << c.hpos[j];
+    return o;
+}
+
 // All threads: one tile of the current job — TMA row loads, micro-ops in
 // shared memory, TMA row stores. Returns false if a wait ran out.
 template <typename T, int A>
@@ -790,7 +792,7 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
         if (lane == 0) mbar_expect_tx(&c.bar, 2u * rows * row_bytes);
         __syncwarp();
         for (uint32_t r = lane; r < rows; r += 32) {
-            const uint64_t gi = base | c.row_off[r];
+            const uint64_t gi = base | row_offset(c, r);
             bulk_load(sre + (size_t)r * row_elems, re + gi, row_bytes, &c.bar);
             bulk_load(sim + (size_t)r * row_elems, im + gi, row_bytes, &c.bar);
         }
@@ -828,7 +830,7 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
     __syncthreads();
     if (warp == 0) {
         for (uint32_t r = lane; r < rows; r += 32) {
-            const uint64_t gi = base | c.row_off[r];
+            const uint64_t gi = base | row_offset(c, r);
             bulk_store(re + gi, sre + (size_t)r * row_elems, row_bytes);
             bulk_store(im + gi, sim + (size_t)r * row_elems, row_bytes);
         }

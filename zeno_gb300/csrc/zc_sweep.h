@@ -6,7 +6,7 @@
 namespace zc {
 
 constexpr uint32_t kOuterFlag = 0x80000000u;  // operand names a non-local qubit (global position)
-constexpr int kMaxMicroOps = 32;               // ops per sweep
+constexpr int kMaxMicroOps = 40;               // ops per sweep
 constexpr uint32_t kMaxSweepHigh = 7;          // chosen high qubits per tile
 constexpr size_t kSweepSmemBytes = 64 * 1024;  // one tile buffer: 2^12 f64 or 2^13 f32 (re + im)
 

@@ -126,6 +126,36 @@ def test_fast_mode_f64_within_1e12(zc, oracle, n):
         g.close()
 
 
+@pytest.mark.parametrize("n", (15, 20))
+def test_fast_mode_f64_general_matrices(zc, oracle, n):
+    """The fast f64 lowering keeps a one-qubit matrix whole when its phases do
+    not split as diagonal * real * diagonal, and uses a general real 2x2 when
+    the real factor is not a rotation: both inside register passes, within
+    1e-12 of the oracle relative to the largest amplitude."""
+    rng = np.random.default_rng(n)
+    amps = rand_state(n, 9, normalize=True)
+    ops = []
+    for i in range(160):
+        q = int(rng.integers(0, n))
+        u = np.linalg.qr(rand_matrix(2, 7000 + i))[0]
+        kind = i % 4
+        if kind == 1:
+            u = u.copy()
+            u[0, 1] *= 1j  # phases no diagonal * real * diagonal gives
+        elif kind == 2:
+            u = u.copy()
+            u[0, 1] *= 0.5  # a real factor that is not a rotation
+        ops.append(("u", [q], u))
+        if kind == 3:
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            ops.append(("cx", a, b))
+    g, o = replay(zc, oracle, n, 64, ops, zc.FLAG_FAST, amps)
+    want = o.statevector()
+    d = np.abs(g.statevector() - want).max() / np.abs(want).max()
+    assert d < 1e-12, d
+    g.close()
+
+
 def test_fast_mode_f32_within_1e5(zc, oracle):
     n = 18
     p = C.matching_circuit(n, 10, 3).to_program()

@@ -42,14 +42,13 @@ SWEEP_DF_PIPES = {"issue_active_pct": 59.4, "fma_pipe_pct": 38.5, "alu_pipe_pct"
 # (zeno_gb300/csrc/zc_arith.cuh): a product is 4 (FMUL + 3 FFMA), TwoSum 6,
 # renormalisation 3. Complex 2x2: four 4-term dot products per pair
 # (4*4 + 3*6 + 6 + 3 = 43 each) = 86; real 2x2 and one-qubit diagonals:
-# 2-term dot products (2*4 + 6 + 2 + 3 = 19), two per amplitude = 38. Inside
-# a register pass the table diagonal and the rotations chain unnormalised
-# pairs: table diagonal 2 x (2*4 + 6 + 2) = 32, rotation [[1, -t], [t, 1]]
-# 2 x (4 + 6 + 2) = 24, plus the pass's one renormalisation (2 x 3 per
-# amplitude) shared by its (usually three) rotations: 26. CX and SWAP move
+# 2-term dot products (2*4 + 6 + 2 + 3 = 19), two per amplitude = 38. Register
+# passes chain unnormalised pairs: table diagonal 2 x (2*4 + 6 + 2) = 32,
+# rotation [[1, -t], [t, 1]] 2 x (4 + 6 + 2) = 24 (one renormalisation per
+# sweep, where the tile goes back to f64, is not counted). CX and SWAP move
 # data only.
 DF_FP32_INSTR_PER_AMP = {"complex": 86, "diag1": 38, "diag_table": 32, "cx": 0, "swap": 0, "real": 38,
-                         "rotation": 26}
+                         "rotation": 24}
 FP32_INSTR_PEAK = 34.3e12  # measured FMA issue rate (zeno_gb300/probes/fp_peaks.cu)
 
 

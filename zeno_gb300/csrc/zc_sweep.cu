@@ -480,7 +480,9 @@ __device__ void run_pass(const GroupInfo &gi, float2 *sr, float2 *si, const OpHe
             }
         }
         // the diagonal and the rotations chain unnormalised pairs (every
-        // double-float op here accepts them); renormalised once at the store
+        // double-float op accepts them; |lo| grows by about an ulp of hi per
+        // op, so the absolute error stays at the double-float bound);
+        // renormalised only where the tile goes back to f64
 #pragma unroll
         for (int g = 0; g < G; g++) {
             if (ROT_ONLY || ops[o + g].kind == MOP_RT) {
@@ -514,9 +516,9 @@ __device__ void run_pass(const GroupInfo &gi, float2 *sr, float2 *si, const OpHe
             if (out_f64) {
                 reinterpret_cast<double *>(sr)[w] = df_to_f64(df_renorm(xr[e]));
                 reinterpret_cast<double *>(si)[w] = df_to_f64(df_renorm(xi[e]));
-            } else {
-                sr[w] = df_renorm(xr[e]);
-                si[w] = df_renorm(xi[e]);
+            } else {  // the next pass accepts unnormalised pairs
+                sr[w] = xr[e];
+                si[w] = xi[e];
             }
         }
     }
@@ -817,10 +819,10 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
         }
         apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut, c.gi, c.fuse_in,
                                 c.fuse_out);
-        if (c.has_arith && !c.fuse_out) {
+        if (c.has_arith && !c.fuse_out) {  // register passes leave pairs unnormalised
             for (uint32_t v = tid; v < size; v += blockDim.x) {
-                dr[v] = df_to_f64(fr[v]);
-                di[v] = df_to_f64(fi[v]);
+                dr[v] = df_to_f64(df_renorm(fr[v]));
+                di[v] = df_to_f64(df_renorm(fi[v]));
             }
         }
     } else {

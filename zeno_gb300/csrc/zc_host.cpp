@@ -702,7 +702,7 @@ int run_batched(const zc_program *p, const zc_run_options *opt, const zc_noise &
     const size_t per_cta = ((size_t)2 << p->n_qubits) * sizeof(float);
     uint64_t budget = 0;
     zc_device_budget(opt->mem_fraction > 0 ? opt->mem_fraction : 0.75, &budget);
-    uint64_t ctas = std::min<uint64_t>(ntraj, (uint64_t)ctx->num_sms * 2);
+    uint64_t ctas = std::min<uint64_t>(ntraj, (uint64_t)ctx->num_sms * 4);  // four trajectories per SM
     ctas = std::min<uint64_t>(ctas, std::max<uint64_t>(1, budget / std::max<size_t>(per_cta, 1)));
     void *d_work = nullptr, *d_buf = nullptr;
     const size_t ops_b = tops.size() * sizeof(TrajOp), mats_b = mats.size() * sizeof(double);

@@ -27,7 +27,7 @@
 namespace zc {
 namespace {
 
-constexpr int kTrajThreads = 512;
+constexpr int kTrajThreads = 256;  // four CTAs (trajectories) per SM at 64 registers
 
 // ---------------------------------------------------------------- Philox4x32-10
 
@@ -64,8 +64,12 @@ __device__ __forceinline__ uint64_t philox_range(uint64_t seed, uint64_t t, uint
 
 // ---------------------------------------------------------------- complex helpers
 
+// Complex values of the per-op operators (gate x Pauli string, pending noise
+// operators, diagonal factors): single precision, like the f32 states they act
+// on (GB300's FP64 pipe would make thread 0's serial work the bottleneck);
+// branch probabilities stay FP64.
 struct C2 {
-    double re, im;
+    float re, im;
 };
 __device__ __forceinline__ C2 cmul(C2 a, C2 b) { return C2{a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re}; }
 __device__ __forceinline__ C2 cadd(C2 a, C2 b) { return C2{a.re + b.re, a.im + b.im}; }
@@ -194,8 +198,60 @@ __device__ void reduce_table(Shared &s, const float *hi, const float *lo, int cn
     __syncthreads();
 }
 
+// One op's pass for a K-qubit op (K = 1, 2, so the group's amplitudes and
+// its probability table stay in registers): the pending diagonal factors,
+// then the gate, accumulating |amplitude|^2 per group row into (hi, lo).
+template <int K, typename T>
+__device__ __forceinline__ void traj_pass(T *re, T *im, uint64_t len, const TrajOp &op, const Shared &s, float *hi,
+                                          float *lo) {
+    constexpr uint32_t D = 1u << K;
+    uint32_t qs[K];
+#pragma unroll
+    for (int b = 0; b < K; b++) qs[b] = op.qs[b];
+    float h[D], l[D];
+#pragma unroll
+    for (uint32_t r = 0; r < D; r++) h[r] = l[r] = 0.f;
+    const uint64_t groups = len >> K;
+    for (uint64_t g = threadIdx.x; g < groups; g += blockDim.x) {
+        const uint64_t base = insert_zeros(g, qs, K);
+        float xr[D], xi[D];
+#pragma unroll
+        for (uint32_t j = 0; j < D; j++) {
+            uint64_t idx = base;
+#pragma unroll
+            for (int b = 0; b < K; b++) idx |= (uint64_t)((j >> b) & 1) << qs[b];
+            float fr, fi;
+            diag_factor(s, idx, fr, fi);
+            const float a = (float)re[idx], c = (float)im[idx];
+            xr[j] = fr * a - fi * c;
+            xi[j] = fr * c + fi * a;
+        }
+#pragma unroll
+        for (uint32_t r = 0; r < D; r++) {
+            float yr = 0.f, yi = 0.f;
+#pragma unroll
+            for (uint32_t c = 0; c < D; c++) {
+                const float wr = s.mr[r * D + c], wi = s.mi[r * D + c];
+                yr = fmaf(wr, xr[c], fmaf(-wi, xi[c], yr));
+                yi = fmaf(wr, xi[c], fmaf(wi, xr[c], yi));
+            }
+            uint64_t idx = base;
+#pragma unroll
+            for (int b = 0; b < K; b++) idx |= (uint64_t)((r >> b) & 1) << qs[b];
+            re[idx] = (T)yr;
+            im[idx] = (T)yi;
+            acc_p2(yr, yi, h[r], l[r]);
+        }
+    }
+#pragma unroll
+    for (uint32_t r = 0; r < D; r++) {
+        hi[r] = h[r];
+        lo[r] = l[r];
+    }
+}
+
 template <typename T>
-__global__ void __launch_bounds__(kTrajThreads)
+__global__ void __launch_bounds__(kTrajThreads, 4)
     k_trajectories(T *__restrict__ work, uint32_t n, const TrajOp *__restrict__ ops, int nops,
                    const double *__restrict__ mats, const uint32_t *__restrict__ fq, const uint32_t *__restrict__ fc,
                    int nfinal, TrajNoise nz, uint64_t ntraj, uint64_t seed, uint64_t *__restrict__ out,
@@ -237,22 +293,32 @@ __global__ void __launch_bounds__(kTrajThreads)
                 if (pdep > 0.0 && philox_f64(seed, t, s.draw++) < pdep)
                     idx = 1 + philox_range(seed, t, s.draw++, (1ull << (2 * k)) - 1);
                 const double *M = mats + op.mat_off;
+                // P_string . M: the Pauli string is a signed permutation, row r
+                // holding its one entry in column r ^ xm (X and Y flip the bit),
+                // of value prod_b v_b(r_b) (Y: -i on 0, i on 1; Z: -1 on 1)
+                uint32_t xm = 0;
+                for (uint32_t b = 0; b < k; b++) {
+                    const uint32_t code = (uint32_t)(idx >> (2 * b)) & 3u;
+                    if (code == 1 || code == 2) xm |= 1u << b;
+                }
                 for (uint32_t r = 0; r < dim; r++) {
-                    for (uint32_t c = 0; c < dim; c++) {
-                        // (P_string . M)[r][c] = sum_j P[r][j] M[j][c]; P is a tensor product of Paulis
-                        C2 acc{0, 0};
-                        for (uint32_t j = 0; j < dim; j++) {
-                            C2 pf{1, 0};
-                            for (uint32_t b = 0; b < k; b++) {
-                                C2 pm[4];
-                                pauli((int)((idx >> (2 * b)) & 3), pm);
-                                pf = cmul(pf, pm[((r >> b) & 1) * 2 + ((j >> b) & 1)]);
-                            }
-                            if (pf.re == 0 && pf.im == 0) continue;
-                            acc = cadd(acc, cmul(pf, C2{M[2 * (j * dim + c)], M[2 * (j * dim + c) + 1]}));
+                    int re_sign = 1, swap = 0;  // phase = re_sign * (swap ? i : 1)
+                    for (uint32_t b = 0; b < k; b++) {
+                        const uint32_t code = (uint32_t)(idx >> (2 * b)) & 3u, rb = (r >> b) & 1u;
+                        if (code == 2) {  // multiply by -i (rb = 0) or i (rb = 1)
+                            if (swap) re_sign = rb ? -re_sign : re_sign;  // i * i = -1, i * -i = 1
+                            else re_sign = rb ? re_sign : -re_sign;
+                            swap ^= 1;
+                        } else if (code == 3 && rb) {
+                            re_sign = -re_sign;
                         }
-                        s.mr[r * dim + c] = (float)acc.re;
-                        s.mi[r * dim + c] = (float)acc.im;
+                    }
+                    const uint32_t j = r ^ xm;
+                    for (uint32_t c = 0; c < dim; c++) {
+                        const float mr = (float)M[2 * (j * dim + c)], mi = (float)M[2 * (j * dim + c) + 1];
+                        // (re_sign * (swap ? i : 1)) * (mr + i mi)
+                        s.mr[r * dim + c] = swap ? -re_sign * mi : re_sign * mr;
+                        s.mi[r * dim + c] = swap ? re_sign * mr : re_sign * mi;
                     }
                 }
             }
@@ -260,31 +326,37 @@ __global__ void __launch_bounds__(kTrajThreads)
             if (s.nondiag) apply_nondiag_pending(re, im, n, s);
             // ---- one pass: pending diagonal factors, gate, joint table
             float hi[8] = {0}, lo[8] = {0};
-            const uint64_t groups = len >> k;
-            for (uint64_t g = tid; g < groups; g += blockDim.x) {
-                const uint64_t base = insert_zeros(g, op.qs, (int)k);
-                float xr[8], xi[8];
-                for (uint32_t j = 0; j < dim; j++) {
-                    uint64_t idx = base;
-                    for (uint32_t b = 0; b < k; b++) idx |= (uint64_t)((j >> b) & 1) << op.qs[b];
-                    float fr, fi;
-                    diag_factor(s, idx, fr, fi);
-                    const float a = (float)re[idx], c = (float)im[idx];
-                    xr[j] = fr * a - fi * c;
-                    xi[j] = fr * c + fi * a;
-                }
-                for (uint32_t r = 0; r < dim; r++) {
-                    float yr = 0.f, yi = 0.f;
-                    for (uint32_t c = 0; c < dim; c++) {
-                        const float wr = s.mr[r * dim + c], wi = s.mi[r * dim + c];
-                        yr = fmaf(wr, xr[c], fmaf(-wi, xi[c], yr));
-                        yi = fmaf(wr, xi[c], fmaf(wi, xr[c], yi));
+            if (k == 1) {
+                traj_pass<1>(re, im, len, op, s, hi, lo);
+            } else if (k == 2) {
+                traj_pass<2>(re, im, len, op, s, hi, lo);
+            } else {  // three-qubit ops (rare): generic loop
+                const uint64_t groups = len >> k;
+                for (uint64_t g = tid; g < groups; g += blockDim.x) {
+                    const uint64_t base = insert_zeros(g, op.qs, (int)k);
+                    float xr[8], xi[8];
+                    for (uint32_t j = 0; j < dim; j++) {
+                        uint64_t idx = base;
+                        for (uint32_t b = 0; b < k; b++) idx |= (uint64_t)((j >> b) & 1) << op.qs[b];
+                        float fr, fi;
+                        diag_factor(s, idx, fr, fi);
+                        const float a = (float)re[idx], c = (float)im[idx];
+                        xr[j] = fr * a - fi * c;
+                        xi[j] = fr * c + fi * a;
                     }
-                    uint64_t idx = base;
-                    for (uint32_t b = 0; b < k; b++) idx |= (uint64_t)((r >> b) & 1) << op.qs[b];
-                    re[idx] = (T)yr;
-                    im[idx] = (T)yi;
-                    acc_p2(yr, yi, hi[r], lo[r]);
+                    for (uint32_t r = 0; r < dim; r++) {
+                        float yr = 0.f, yi = 0.f;
+                        for (uint32_t c = 0; c < dim; c++) {
+                            const float wr = s.mr[r * dim + c], wi = s.mi[r * dim + c];
+                            yr = fmaf(wr, xr[c], fmaf(-wi, xi[c], yr));
+                            yi = fmaf(wr, xi[c], fmaf(wi, xr[c], yi));
+                        }
+                        uint64_t idx = base;
+                        for (uint32_t b = 0; b < k; b++) idx |= (uint64_t)((r >> b) & 1) << op.qs[b];
+                        re[idx] = (T)yr;
+                        im[idx] = (T)yi;
+                        acc_p2(yr, yi, hi[r], lo[r]);
+                    }
                 }
             }
             __syncthreads();
@@ -299,9 +371,9 @@ __global__ void __launch_bounds__(kTrajThreads)
                 Pending &P = s.pend[s.npend++];
                 P.q = op.qs[0];
                 for (int i = 0; i < 4; i++) P.m[i] = C2{0, 0};
-                if (!one) P.m[0] = C2{sc, 0};
-                else if (op.kind == TOP_RESET) P.m[1] = C2{sc, 0};  // X . diag(0, sc)
-                else P.m[3] = C2{sc, 0};
+                if (!one) P.m[0] = C2{(float)sc, 0};
+                else if (op.kind == TOP_RESET) P.m[1] = C2{(float)sc, 0};  // X . diag(0, sc)
+                else P.m[3] = C2{(float)sc, 0};
                 if (op.kind == TOP_MEASURE) {
                     bool bit = one;
                     const double pr = bit ? nz.p[6] : nz.p[5];  // readout_flip (src/noise.rs:181-192)
@@ -344,7 +416,7 @@ __global__ void __launch_bounds__(kTrajThreads)
                         C2 D[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
                         if (u < pj) {
                             // jump: collapse to 1 (scale 1/sqrt(P1)) then X
-                            D[1] = C2{1.0 / sqrt(p1), 0};
+                            D[1] = C2{(float)(1.0 / sqrt(p1)), 0};
                             for (uint32_t j = 0; j < dim; j++)
                                 if (!((j >> b) & 1)) {
                                     J[j] = J[j | (1u << b)] / p1;
@@ -352,9 +424,10 @@ __global__ void __launch_bounds__(kTrajThreads)
                                 }
                         } else {
                             const double sc = 1.0 / sqrt(1.0 - pj);
-                            D[0] = C2{sc, 0};
-                            D[3] = C2{sc * sqrt(1.0 - nz.p[4]), 0};
-                            for (uint32_t j = 0; j < dim; j++) J[j] *= ((j >> b) & 1) ? D[3].re * D[3].re : sc * sc;
+                            const double d3 = sc * sqrt(1.0 - nz.p[4]);
+                            D[0] = C2{(float)sc, 0};
+                            D[3] = C2{(float)d3, 0};
+                            for (uint32_t j = 0; j < dim; j++) J[j] *= ((j >> b) & 1) ? d3 * d3 : sc * sc;
                         }
                         mul22(D, M, M);
                     }

@@ -34,10 +34,10 @@ sys.path.insert(0, ROOT)
 HBM_FALLBACK_GBS = 6800.0
 # DRAM read+write per launch over algorithmic bytes, from an ncu capture of
 # the f64 double-float sweep kernel at 26 qubits (state 8x the L2):
-# 1.074 GB read + 1.023 GB write against 2S = 2.147 GB.
-MEASURED_TRAFFIC_RATIO = {"sweep": (1.074e9 + 1.023e9) / 2.147e9}
-# The same capture: issue slots 59% busy, FMA pipe 38%, ALU pipe 31%, FP64 0%.
-SWEEP_DF_PIPES = {"issue_active_pct": 59.4, "fma_pipe_pct": 38.5, "alu_pipe_pct": 30.7, "fp64_pipe_pct": 0.0}
+# 1.074 GB read + 1.027 GB write against 2S = 2.147 GB.
+MEASURED_TRAFFIC_RATIO = {"sweep": (1.074e9 + 1.027e9) / 2.147e9}
+# The same capture: issue slots 58% busy, FMA pipe 37%, ALU pipe 31%, FP64 0%.
+SWEEP_DF_PIPES = {"issue_active_pct": 57.6, "fma_pipe_pct": 36.5, "alu_pipe_pct": 30.9, "fp64_pipe_pct": 0.0}
 # FP32 instructions per amplitude of each double-float sweep micro-op
 # (zeno_gb300/csrc/zc_arith.cuh): a product is 4 (FMUL + 3 FFMA), TwoSum 6,
 # renormalisation 3. Complex 2x2: four 4-term dot products per pair

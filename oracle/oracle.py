@@ -3,8 +3,8 @@
 Loads `oracle/_build/libzeno_oracle.so` (the C restatement of zeno's scalar
 CPU backend, sampler, executor, noise channels, gate library and compiler;
 see zeno_oracle.h for the reference file:line map).  Only the tests,
-`__graft_entry__.smoke()` and the CPU-baseline leg of `bench.py` use it, as
-the checker; the shipped library never does.
+`__graft_entry__.smoke()` and the CPU-baseline leg of `bench.py` use it, to
+check results and to time the CPU baseline; the shipped library never does.
 """
 
 from __future__ import annotations

@@ -208,6 +208,9 @@ __device__ __forceinline__ void traj_pass(T *re, T *im, uint64_t len, const Traj
     uint32_t qs[K];
 #pragma unroll
     for (int b = 0; b < K; b++) qs[b] = op.qs[b];
+    // the op matrix is read from shared memory at each use: hoisted into
+    // registers it would spill at the 64-register cap of four CTAs per SM
+    const volatile float *mr = s.mr, *mi = s.mi;
     float h[D], l[D];
 #pragma unroll
     for (uint32_t r = 0; r < D; r++) h[r] = l[r] = 0.f;
@@ -231,7 +234,7 @@ __device__ __forceinline__ void traj_pass(T *re, T *im, uint64_t len, const Traj
             float yr = 0.f, yi = 0.f;
 #pragma unroll
             for (uint32_t c = 0; c < D; c++) {
-                const float wr = s.mr[r * D + c], wi = s.mi[r * D + c];
+                const float wr = mr[r * D + c], wi = mi[r * D + c];
                 yr = fmaf(wr, xr[c], fmaf(-wi, xi[c], yr));
                 yi = fmaf(wr, xi[c], fmaf(wi, xr[c], yi));
             }

@@ -5,89 +5,11 @@
 // fused table diagonal indexed from the descriptor, gates in order, flipped
 // stores), and the tile must equal the micro-ops applied one by one. Outer
 // qubits (outside the tile) take their values from a fixed tile base.
-#include <cmath>
-#include <complex>
-#include <cstdio>
-#include <random>
-#include <vector>
+#include "tile_ref.h"
 
-#include "zc_passes.h"
-
-using cd = std::complex<double>;
-using zc::OpHead;
+using namespace tile_ref;
 
 namespace {
-
-constexpr uint32_t T = 9;  // tile bits
-constexpr uint32_t kSize = 1u << T;
-constexpr uint32_t kOuter0 = 20, kNOuter = 6;  // outer qubits 20..25
-uint64_t g_base = 0;                           // the tile's outer qubit values
-
-struct Op {
-    OpHead h;
-    double m[8];
-    std::vector<cd> tab;  // DK table
-};
-
-uint32_t bit_of(uint32_t slot, uint32_t x) {
-    return x & zc::kOuterFlag ? (uint32_t)((g_base >> (x & ~zc::kOuterFlag)) & 1) : (slot >> x) & 1;
-}
-
-void apply_pair(std::vector<cd> &s, uint32_t a, const cd u[4]) {
-    for (uint32_t i = 0; i < kSize; i++)
-        if (!((i >> a) & 1)) {
-            const uint32_t j = i | (1u << a);
-            const cd x = s[i], y = s[j];
-            s[i] = u[0] * x + u[1] * y;
-            s[j] = u[2] * x + u[3] * y;
-        }
-}
-
-void gate_matrix(const Op &op, cd u[4]) {
-    const OpHead &h = op.h;
-    if (h.kind == zc::MOP_U1) {
-        for (int i = 0; i < 4; i++) u[i] = cd(op.m[2 * i], op.m[2 * i + 1]);
-    } else if (h.kind == zc::MOP_R1) {
-        for (int i = 0; i < 4; i++) u[i] = op.m[i];
-    } else {  // RT: [[1, -t], [t, 1]], rows swapped when flipped
-        const double t = op.m[0];
-        const cd r[4] = {1.0, -t, t, 1.0};
-        if (h.b) {
-            u[0] = r[2], u[1] = r[3], u[2] = r[0], u[3] = r[1];
-        } else {
-            for (int i = 0; i < 4; i++) u[i] = r[i];
-        }
-    }
-}
-
-void apply_one(std::vector<cd> &s, const Op &op) {
-    const OpHead &h = op.h;
-    switch (h.kind) {
-        case zc::MOP_U1:
-        case zc::MOP_R1:
-        case zc::MOP_RT: {
-            cd u[4];
-            gate_matrix(op, u);
-            apply_pair(s, h.a, u);
-            break;
-        }
-        case zc::MOP_DK:
-            for (uint32_t i = 0; i < kSize; i++) {
-                uint32_t j = 0;
-                for (uint32_t b = 0; b < h.k; b++) j |= bit_of(i, h.loc[b]) << b;
-                s[i] *= op.tab[j];
-            }
-            break;
-        case zc::MOP_CX:
-            for (uint32_t i = 0; i < kSize; i++)
-                if (bit_of(i, h.a) && !((i >> h.b) & 1)) std::swap(s[i], s[i | (1u << h.b)]);
-            break;
-        case zc::MOP_SWAP:
-            for (uint32_t i = 0; i < kSize; i++)
-                if (((i >> h.a) & 1) && !((i >> h.b) & 1)) std::swap(s[i], s[(i ^ (1u << h.a)) | (1u << h.b)]);
-            break;
-    }
-}
 
 // One pass, as the kernel's run_pass applies it.
 void apply_pass(std::vector<cd> &s, const zc::GroupInfo &q, const std::vector<Op> &ops) {
@@ -155,97 +77,16 @@ void apply_pass(std::vector<cd> &s, const zc::GroupInfo &q, const std::vector<Op
 }  // namespace
 
 int main() {
-    std::mt19937_64 rng(97531);
-    std::uniform_real_distribution<double> U(-1.0, 1.0);
+    Gen gen(97531);
     double worst = 0.0;
     size_t passes = 0, folded = 0, fused = 0, translations = 0;
     for (int trial = 0; trial < 3000; trial++) {
-        g_base = 0;
-        for (uint32_t i = 0; i < kNOuter; i++)
-            if (rng() & 1) g_base |= 1ull << (kOuter0 + i);
-        auto local = [&]() { return (uint32_t)(rng() % T); };
-        auto outer = [&]() { return zc::kOuterFlag | (kOuter0 + (uint32_t)(rng() % kNOuter)); };
-        std::vector<Op> ops;
-        uint32_t tables = 0;
-        auto add_gate = [&](uint32_t a) {
-            Op op{};
-            const int kind = (int)(rng() % 6);
-            op.h.a = a;
-            if (kind < 4) {
-                op.h.kind = zc::MOP_RT;
-                op.m[0] = U(rng);
-                op.h.b = (uint32_t)(rng() & 1);
-            } else if (kind < 5) {
-                op.h.kind = zc::MOP_R1;
-                for (int i = 0; i < 4; i++) op.m[i] = U(rng);
-            } else {
-                op.h.kind = zc::MOP_U1;
-                for (int i = 0; i < 8; i++) op.m[i] = U(rng);
-            }
-            ops.push_back(op);
-        };
-        auto add_dk = [&]() {
-            Op op{};
-            op.h.kind = zc::MOP_DK;
-            op.h.k = 1 + (uint32_t)(rng() % 6);
-            uint64_t used = 0;
-            for (uint32_t b = 0; b < op.h.k;) {
-                const uint32_t x = rng() % 4 == 0 ? outer() : local();
-                const uint64_t key = x & zc::kOuterFlag ? 1ull << (32 + (x & 31)) : 1ull << x;
-                if (used & key) continue;
-                used |= key;
-                op.h.loc[b++] = x;
-            }
-            op.h.table = tables++;
-            op.tab.resize((size_t)1 << op.h.k);
-            for (auto &w : op.tab) w = std::polar(1.0, 3.0 * U(rng));
-            ops.push_back(op);
-        };
-        auto add_cx = [&](uint32_t t) {
-            Op op{};
-            op.h.kind = zc::MOP_CX;
-            op.h.b = t;
-            do op.h.a = rng() % 3 == 0 ? outer() : local();
-            while (op.h.a == t);
-            ops.push_back(op);
-        };
-        const int len = 4 + (int)(rng() % 30);
-        while ((int)ops.size() < len) {
-            const int r = (int)(rng() % 10);
-            if (r < 4) {  // the lowering's pattern: CX block, table diagonal, run on the targets
-                uint32_t t[3];
-                const int g = 1 + (int)(rng() % 3);
-                for (int i = 0; i < g; i++) {
-                    bool fresh;
-                    do {
-                        t[i] = local();
-                        fresh = true;
-                        for (int j = 0; j < i; j++) fresh &= t[j] != t[i];
-                    } while (!fresh);
-                }
-                const int ncx = (int)(rng() % 4);
-                for (int i = 0; i < ncx; i++) add_cx(t[rng() % g]);
-                if (rng() % 3) add_dk();
-                for (int i = 0; i < g; i++) add_gate(t[i]);
-            } else if (r < 6) {
-                add_gate(local());
-            } else if (r < 7) {
-                add_dk();
-            } else if (r < 9) {
-                add_cx(local());
-            } else {
-                Op op{};
-                op.h.kind = zc::MOP_SWAP;
-                op.h.a = local();
-                do op.h.b = local();
-                while (op.h.b == op.h.a);
-                ops.push_back(op);
-            }
-        }
+        gen.new_base();
+        const std::vector<Op> ops = gen.list(30);
         std::vector<OpHead> heads;
         for (const Op &op : ops) heads.push_back(op.h);
         std::vector<cd> s0(kSize);
-        for (auto &z : s0) z = cd(U(rng), U(rng));
+        for (auto &z : s0) z = cd(gen.U(gen.rng), gen.U(gen.rng));
         std::vector<cd> want = s0;
         for (const Op &op : ops) apply_one(want, op);
         // fold: the one-job kernel (the multi-job kernel plans without it);
@@ -256,7 +97,7 @@ int main() {
             std::vector<zc::GroupInfo> gi(ops.size());
             uint32_t bad = 0;
             int fuse_in = -1, fuse_out = -1;
-            zc::plan_passes(heads.data(), (int)ops.size(), T, fold, max_group, gi.data(), &bad, &fuse_in,
+            zc::plan_passes(heads.data(), (int)ops.size(), kTileBits, fold, max_group, gi.data(), &bad, &fuse_in,
                             &fuse_out);
             if (bad) {
                 std::printf("FAIL trial %d variant %d: planner flagged op %u\n", trial, variant, bad & 0x7fffffffu);
@@ -289,14 +130,10 @@ int main() {
                 std::printf("FAIL trial %d variant %d: fuse flags %d %d\n", trial, variant, fuse_in, fuse_out);
                 return 1;
             }
-            double err = 0.0, scale = 0.0;
-            for (uint32_t i = 0; i < kSize; i++) {
-                err = std::max(err, std::abs(got[i] - want[i]));
-                scale = std::max(scale, std::abs(want[i]));
-            }
-            worst = std::max(worst, err / scale);
-            if (err > 1e-12 * scale) {
-                std::printf("FAIL trial %d variant %d: max |diff| %.3e (scale %.3e)\n", trial, variant, err, scale);
+            const double d = rel_diff(got, want);
+            worst = std::max(worst, d);
+            if (d > 1e-12) {
+                std::printf("FAIL trial %d variant %d: max |diff| %.3e relative\n", trial, variant, d);
                 return 1;
             }
         }

@@ -1,4 +1,4 @@
-"""Register passes of double-float sweeps (no GPU).
+"""Register passes of double-float sweeps, checked on the host (no GPU).
 
 tests/passes_harness.cpp plans random micro-op lists on one 2^9-amplitude
 tile with plan_passes (zeno_gb300/csrc/zc_passes.h, the code the sweep kernel
@@ -25,17 +25,22 @@ def _cuda_include():
     return None
 
 
-def test_passes_apply_the_micro_ops(tmp_path):
+def _run_harness(name, tmp_path):
     cxx = shutil.which("g++")
     inc = _cuda_include()
     if cxx is None or inc is None:
         pytest.skip("g++ or the CUDA headers are missing")
-    exe = str(tmp_path / "passes_harness")
+    exe = str(tmp_path / name)
     subprocess.run([cxx, "-std=c++17", "-O2", "-Wall", "-Werror", "-I" + CSRC, "-I" + inc,
-                    os.path.join(ROOT, "tests", "passes_harness.cpp"), "-o", exe], check=True)
-    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+                    os.path.join(ROOT, "tests", name + ".cpp"), "-o", exe], check=True)
+    return subprocess.run([exe], check=True, capture_output=True, text=True).stdout
+
+
+def test_passes_apply_the_micro_ops(tmp_path):
+    out = _run_harness("passes_harness", tmp_path)
     m = re.match(r"ok worst (\S+) passes (\d+) folded (\d+) fused (\d+) translations (\d+)", out)
     assert m, out
     assert float(m[1]) < 1e-12
     # every feature of the descriptors was exercised
     assert all(int(m[i]) > 1000 for i in range(2, 6)), out
+

@@ -3,12 +3,13 @@
 // The state is cut into tiles of 2^T amplitudes: the L lowest qubits (a
 // contiguous row of 2^L elements, 256 bytes) plus H chosen higher qubits
 // ("local" qubits); the other n - T qubits pick the tile. A persistent CTA
-// streams tiles through two shared-memory buffers: every row of a tile is
+// streams tiles through one shared-memory buffer: every row of a tile is
 // fetched with one TMA bulk copy (cp.async.bulk, completion on an
 // mbarrier), the sweep's micro-ops are applied in shared memory, and the
-// rows go back with TMA bulk stores while the next tile is already in
-// flight. Every micro-op uses the same arithmetic as the per-op kernels, so
-// a sweep is bit-identical to launching its ops one by one.
+// rows go back with TMA bulk stores; three CTAs per SM overlap one tile's
+// copies with the others' arithmetic. Every micro-op uses the same
+// arithmetic as the per-op kernels, so a sweep is bit-identical to
+// launching its ops one by one.
 //
 // Which ops fit a sweep: unitaries whose qubits are all local; diagonals
 // on any qubits (bits of non-local qubits are constant per tile); CX with a

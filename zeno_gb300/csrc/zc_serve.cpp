@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "zc_internal.h"
+#include "zc_pool.h"
 #include "zc_rng.h"
 #include "../../include/zeno_cuda_serve.h"
 #include "zc_sweep.h"
@@ -66,7 +67,7 @@ struct zc_server {
     zc_state *ctx = nullptr;  // stream, parameter arena, reduction scratch, error flag
     char *pool = nullptr;
     size_t pool_bytes = 0;
-    std::vector<std::pair<size_t, size_t>> free_list;  // (offset, length), sorted by offset
+    zc::PoolFreeList free_list;  // offsets of the pool not held by active requests
     uint32_t max_slots = 0;
     uint32_t flags = 0;
     uint64_t next_id = 1;
@@ -89,36 +90,6 @@ struct zc_server {
 
 namespace zc {
 namespace {
-
-bool pool_alloc(zc_server *s, size_t bytes, size_t *off) {
-    for (size_t i = 0; i < s->free_list.size(); i++) {
-        auto &f = s->free_list[i];
-        if (f.second >= bytes) {
-            *off = f.first;
-            f.first += bytes;
-            f.second -= bytes;
-            if (f.second == 0) s->free_list.erase(s->free_list.begin() + (long)i);
-            return true;
-        }
-    }
-    return false;
-}
-
-void pool_free(zc_server *s, size_t off, size_t bytes) {
-    auto &fl = s->free_list;
-    auto it = std::lower_bound(fl.begin(), fl.end(), std::make_pair(off, (size_t)0));
-    it = fl.insert(it, {off, bytes});
-    // merge with neighbours
-    size_t i = (size_t)(it - fl.begin());
-    if (i + 1 < fl.size() && fl[i].first + fl[i].second == fl[i + 1].first) {
-        fl[i].second += fl[i + 1].second;
-        fl.erase(fl.begin() + (long)i + 1);
-    }
-    if (i > 0 && fl[i - 1].first + fl[i - 1].second == fl[i].first) {
-        fl[i - 1].second += fl[i].second;
-        fl.erase(fl.begin() + (long)i);
-    }
-}
 
 // A state view over pool memory that borrows the server context's stream
 // and parameter ring.
@@ -377,7 +348,7 @@ int zc_server_create(const zc_server_options *opt, zc_server **out) {
     s->pool_bytes = opt->pool_bytes ? opt->pool_bytes : budget / 2;
     cudaError_t e = cudaMalloc(&s->pool, s->pool_bytes);
     if (e != cudaSuccess) return bail(fail(ZC_ERR_MEMORY, "server pool allocation failed"));
-    s->free_list.push_back({0, s->pool_bytes});
+    s->free_list.reset(s->pool_bytes);
     for (auto &g : s->groups) {
         for (auto &hb : g.h_blob)
             if ((e = cudaMallocHost(&hb, kBlobBytes)) != cudaSuccess) return bail(cuda_fail(e, "cudaMallocHost"));
@@ -455,7 +426,7 @@ int zc_server_step(zc_server *s, zc_server_status *status) {
     // 1. admission: FIFO, by HBM footprint and free slots
     while (!s->pending.empty() && s->active.size() < s->max_slots) {
         Request *r = s->pending.front();
-        if (!pool_alloc(s, r->bytes, &r->off)) break;
+        if (!s->free_list.alloc(r->bytes, &r->off)) break;
         s->pending.pop_front();
         make_view(s, r);
         if ((rc = launch_reset(&r->view))) return rc;
@@ -492,7 +463,7 @@ int zc_server_step(zc_server *s, zc_server_status *status) {
     }
     if ((rc = sample_finished(s, sampled))) return rc;
     for (Request *r : fin) {
-        pool_free(s, r->off, r->bytes);
+        s->free_list.release(r->off, r->bytes);
         s->done[r->id] = r;
         s->completed++;
     }
@@ -517,9 +488,7 @@ int zc_server_step(zc_server *s, zc_server_status *status) {
         status->packed_launches = s->packed_launches;
         status->admitted = s->admitted;
         status->completed = s->completed;
-        size_t free_b = 0;
-        for (auto &f : s->free_list) free_b += f.second;
-        status->pool_used = s->pool_bytes - free_b;
+        status->pool_used = s->pool_bytes - s->free_list.free_bytes();
         status->steps = s->steps;
         status->plan_us = s->plan_us;
         status->sample_us = s->sample_us;

@@ -16,51 +16,19 @@
 // order on that table (each decision updates the table) and leaves the
 // resulting 2x2 operators pending for the next pass. All draws of an op are
 // independent of the state, so they are taken up front in the reference's
-// order from a per-trajectory Philox4x32-10 stream (Salmon et al., SC'11).
+// order from a per-trajectory Philox4x32-10 stream (zc_philox.h).
 // Probabilities are summed in double-float per thread and reduced in FP64.
 #include <algorithm>
 
 #include "zc_arith.cuh"
 #include "zc_internal.h"
+#include "zc_philox.h"
 #include "zc_traj.h"
 
 namespace zc {
 namespace {
 
 constexpr int kTrajThreads = 256;  // four CTAs (trajectories) per SM at 64 registers
-
-// ---------------------------------------------------------------- Philox4x32-10
-
-struct U4 {
-    uint32_t x, y, z, w;
-};
-
-__device__ __forceinline__ U4 philox10(U4 c, uint32_t k0, uint32_t k1) {
-#pragma unroll
-    for (int r = 0; r < 10; r++) {
-        const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
-        const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
-        c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
-        k0 += 0x9E3779B9u;
-        k1 += 0xBB67AE85u;
-    }
-    return c;
-}
-
-// Uniform f64 in [0, 1) from draw number `i` of trajectory `t`.
-__device__ __forceinline__ double philox_f64(uint64_t seed, uint64_t t, uint64_t i) {
-    const U4 r = philox10(U4{(uint32_t)i, (uint32_t)(i >> 32), (uint32_t)t, (uint32_t)(t >> 32)}, (uint32_t)seed,
-                          (uint32_t)(seed >> 32));
-    const uint64_t bits = ((uint64_t)(r.x >> 5) << 26) | (uint64_t)(r.y >> 6);
-    return (double)bits * (1.0 / 9007199254740992.0);
-}
-
-__device__ __forceinline__ uint64_t philox_range(uint64_t seed, uint64_t t, uint64_t i, uint64_t n) {
-    const U4 r = philox10(U4{(uint32_t)i, (uint32_t)(i >> 32), (uint32_t)t, (uint32_t)(t >> 32)}, (uint32_t)seed,
-                          (uint32_t)(seed >> 32));
-    const uint64_t v = ((uint64_t)r.z << 32) | r.w;
-    return (uint64_t)(((unsigned __int128)v * n) >> 64);  // multiply-shift, bias < n / 2^64
-}
 
 // ---------------------------------------------------------------- complex helpers
 

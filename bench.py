@@ -365,6 +365,9 @@ def main():
                    "ops": len(ops), "input_gates": prog.stats["input_gates"]},
         "gpu_launches": int(c1["launches"] - c0["launches"]),
         "gpu_busy_frac": gates_ms / 1000.0 / elapsed,
+        "amp_updates_per_s": {"value": prog.stats["input_gates"] * 2.0 ** a.qubits * value,
+                              "definition": "input gates x 2^n per second, the throughput zeno bench prints "
+                                            "(src/main.rs:1138)"},
         "kernels": {c: {"launches": d["launches"], "avg_ms": d["ms"] / d["launches"],
                         "GBps": (d["bytes"] / d["launches"]) / (d["ms"] / d["launches"] / 1000.0) / 1e9
                         if d["bytes"] else None,

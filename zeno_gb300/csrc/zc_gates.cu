@@ -3,6 +3,7 @@
 // im[] of 2^n elements), every global access a 16-byte vector where the
 // index pattern allows it.
 #include <algorithm>
+#include <atomic>
 
 #include "zc_arith.cuh"
 #include "zc_internal.h"
@@ -189,7 +190,7 @@ int run_kq(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat) {
     }
     const int G = kKqTile / dim;
     const size_t smem = (size_t)4 * G * (dim + 1) * sizeof(T);
-    static bool attr_set[2] = {false, false};
+    static std::atomic<bool> attr_set[2] = {{false}, {false}};  // per precision, once per process
     if (!attr_set[sizeof(T) == 8]) {
         ZC_CUDA(cudaFuncSetAttribute(k_kq<T, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize, 160 * 1024));
         attr_set[sizeof(T) == 8] = true;
@@ -320,7 +321,7 @@ int run_diagk(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_diag
     if (st->len < (uint64_t)V) {
         k_diag_scalar<T, A><<<1, 64, 0, st->stream>>>(re, im, st->len, p, dre, dim_);
     } else {
-        static bool attr_set[2] = {false, false};
+        static std::atomic<bool> attr_set[2] = {{false}, {false}};  // per precision, once per process
         if (!attr_set[sizeof(T) == 8]) {
             ZC_CUDA(cudaFuncSetAttribute(k_diagk<T, A>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
             attr_set[sizeof(T) == 8] = true;

@@ -14,6 +14,8 @@
 // at every 32-element stage boundary; draws then resolve in parallel by a
 // binary search over those values and a replay of one stage, which repeats
 // the chain's own additions bit for bit.
+#include <atomic>
+
 #include "zc_arith.cuh"
 #include "zc_internal.h"
 
@@ -394,7 +396,7 @@ __global__ void __launch_bounds__(kDfThreads) k_sample_scan_df(const T *__restri
 template <typename T, bool SCAN>
 int run_chain(zc_state *st, unsigned blocks, uint64_t total, uint64_t chunk, uint64_t nrows, int mode, uint32_t q,
               const SampleChunk *cs, const double *us, double *part, double *rec, uint32_t stride) {
-    static bool attr = false;
+    static std::atomic<bool> attr{false};  // set once per process; racing first calls repeat it
     if (!attr) {
         ZC_CUDA(cudaFuncSetAttribute(k_chain<T, SCAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kChainSmem));
         attr = true;

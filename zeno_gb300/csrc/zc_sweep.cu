@@ -14,6 +14,7 @@
 // Which ops fit a sweep: unitaries whose qubits are all local; diagonals
 // on any qubits (bits of non-local qubits are constant per tile); CX with a
 // local target and any control; SWAP of two local qubits.
+#include <atomic>
 #include <algorithm>
 
 #include "zc_arith.cuh"
@@ -747,7 +748,7 @@ __global__ void __launch_bounds__(kSweepThreads, kSweepCtasPerSm)
 template <typename T, int A>
 int run_sweep(zc_state *st, const SweepGeom &g, const MicroOp *dev_ops, int nops, const char *dev_tables) {
     const size_t smem = (size_t)2 * (1u << (g.L + g.H)) * sizeof(T);
-    static bool attr = false;
+    static std::atomic<bool> attr{false};  // set once per process; racing first calls repeat it
     if (!attr) {
         ZC_CUDA(cudaFuncSetAttribute(k_sweep<T, A>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)kSweepSmemBytes));
@@ -764,7 +765,7 @@ int run_sweep(zc_state *st, const SweepGeom &g, const MicroOp *dev_ops, int nops
 
 template <typename T, int A>
 int run_sweep_multi(cudaStream_t stream, int num_sms, const char *dev_blob, int *d_err) {
-    static bool attr = false;
+    static std::atomic<bool> attr{false};  // set once per process; racing first calls repeat it
     if (!attr) {
         ZC_CUDA(cudaFuncSetAttribute(k_sweep_multi<T, A>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)kSweepSmemBytes));

@@ -22,6 +22,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <atomic>
 #include <vector>
 
 #include "zc_arith.cuh"
@@ -160,7 +161,7 @@ template <int R>
 int run_tc(zc_state *st, const TcParams &p, const float *ah, const float *al) {
     constexpr int SL = R < kTcSlice ? R : kTcSlice;
     const size_t smem = (size_t)(2 * R * (kTcCols + kTcPad) + 2 * R * (SL + kTcPad)) * sizeof(float);
-    static bool attr = false;
+    static std::atomic<bool> attr{false};  // set once per process; racing first calls repeat it
     if (!attr) {
         ZC_CUDA(cudaFuncSetAttribute(k_block_tc<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
@@ -434,12 +435,15 @@ __global__ void __launch_bounds__(kUmThreads, R <= 64 ? 2 : 1)
 template <int R>
 int run_umma(zc_state *st, const TcParams &p, const float *a) {
     constexpr size_t smem = umma_smem_bytes(R);
-    static bool attr = false;
+    static std::atomic<bool> attr{false};  // set once per process; racing first calls repeat it
     if (!attr) {
         ZC_CUDA(cudaFuncSetAttribute(k_block_umma<R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr = true;
     }
-    static int per_sm = 0;  // resident CTAs per SM: shared memory, registers and tensor memory decide
+    // resident CTAs per SM (shared memory, registers and tensor memory
+    // decide), found once per process
+    static std::atomic<int> cached_per_sm{0};
+    int per_sm = cached_per_sm.load();
     if (!per_sm) {
         ZC_CUDA(cudaFuncSetAttribute(k_block_umma<R>, cudaFuncAttributePreferredSharedMemoryCarveout,
                                      (int)cudaSharedmemCarveoutMaxShared));
@@ -453,6 +457,7 @@ int run_umma(zc_state *st, const TcParams &p, const float *a) {
         const int by_regs = regs_sm / std::max(1, fa.numRegs * kUmThreads);
         per_sm = std::min(std::min(by_smem, by_regs), 512 / R);
         if (per_sm < 1) return fail(ZC_ERR_UNSUPPORTED, "tensor-core block kernel does not fit on an SM");
+        cached_per_sm.store(per_sm);
     }
     const uint64_t ntiles = (p.groups + kUmM - 1) / kUmM;
     const int blocks = (int)std::min<uint64_t>(ntiles, (uint64_t)st->num_sms * per_sm);

@@ -297,6 +297,28 @@ def test_noise_closed_forms(oracle):
     six_sigma(counts.get("0", 0), shots, 0.2)
 
 
+def test_noise_two_qubit_and_phase_closed_forms(oracle):
+    """tests/noise.rs:312-384: a depolarizing hit on CX draws one of the 15
+    non-identity Pauli strings, so |00> changes with probability 12p/15 and
+    the Bell parity flips with 8p/15 (<ZZ> = 1 - 16p/15); a phase flip after
+    H shows up as P(1) = p once RY(-pi/2) maps |+>, |-> to |0>, |1> (H H
+    would cancel in the compiler and carry no noise)."""
+    shots, p = 20000, 0.3
+    c = C.Circuit(2)
+    c.cx(0, 1).measure(0, 0).measure(1, 1)
+    counts, _, _, _ = oracle.run(c.to_program(), shots=shots, seed=21, noise=_N(depolarizing_2q=p))
+    six_sigma(shots - counts.get("00", 0), shots, 12 * p / 15)
+    c = C.Circuit(2)
+    c.h(0).cx(0, 1).measure(0, 0).measure(1, 1)
+    counts, _, _, _ = oracle.run(c.to_program(), shots=shots, seed=22, noise=_N(depolarizing_2q=p))
+    odd = counts.get("01", 0) + counts.get("10", 0)
+    six_sigma(odd, shots, 8 * p / 15)
+    c = C.Circuit(1)
+    c.h(0).ry(0, -math.pi / 2).measure(0, 0)
+    counts, _, _, _ = oracle.run(c.to_program(), shots=shots, seed=23, noise=_N(phase_flip=0.2))
+    six_sigma(counts.get("1", 0), shots, 0.2)
+
+
 def _damp_p1(g):
     """P(1) after x, then 3 x (sx, sxdg) pairs with damping after each of the 7 gates.
 

@@ -87,3 +87,36 @@ def test_compile_errors(zc):
     c.gate("h", [5])
     with pytest.raises(zc.ZenoCudaError, match="out of range"):
         zc.compile(c.to_program())
+
+
+def _cancel_case(build, n=3):
+    c = C.Circuit(n)
+    build(c)
+    return c.to_program()
+
+
+@pytest.mark.parametrize("build, cancelled", [
+    (lambda c: c.h(0).h(0), 2),                                    # self-inverse pair
+    (lambda c: c.cx(0, 1).x(2).cx(0, 1), 2),                       # a gate on other qubits does not block
+    (lambda c: c.cx(0, 1).x(1).cx(0, 1), 0),                       # an overlapping gate does
+    (lambda c: c.cx(0, 1).cx(1, 0), 0),                            # same gate, other argument order
+    (lambda c: c.swap(0, 1).swap(1, 0), 0),                        # (also for symmetric gates)
+    (lambda c: c.x(0).h(0).h(0).x(0), 4),                          # nested pairs unwind
+    (lambda c: c.h(0).barrier().h(0), 0),                          # a barrier ends the search
+    (lambda c: c.rx(0, 0.3).rx(0, 0.3), 0),                        # gates with parameters never cancel
+    (lambda c: c.ccx(0, 1, 2).cz(0, 1).ccx(0, 1, 2), 0),
+    (lambda c: c.ccx(0, 1, 2).ccx(0, 1, 2).cz(1, 2).cz(1, 2), 4),
+])
+def test_cancellation_identities(zc, oracle, build, cancelled):
+    """compiler::cancel (src/compiler.rs:215-239): a parameterless
+    self-inverse gate cancels against the nearest earlier gate that shares a
+    qubit when that gate is the same gate on the same qubits in the same
+    order (tests/analytic.rs cancellation identities)."""
+    p = _cancel_case(build)
+    mine = zc.compile(p, 1, swap_perm=False)
+    assert mine.stats["cancelled"] == cancelled
+    assert oracle.compile(p, 1).stats["cancelled"] == cancelled
+    if cancelled == len(p.instrs):
+        assert mine.ops == []
+    for fusion in (0, 1, 3):
+        _same_ops(zc, oracle, p, fusion)

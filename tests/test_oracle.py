@@ -224,6 +224,32 @@ def test_examples_known_answers(oracle, examples):
             six_sigma(counts[exp["keys"][0]], 4000, exp["p"])
 
 
+def test_analytic_statistics(oracle):
+    """tests/analytic.rs 6-sigma checks: uniform superposition, reset after
+    entanglement, mid-circuit measurement feeding a later gate."""
+    shots = 16000
+    c = C.Circuit(4)
+    for q in range(4):
+        c.h(q)
+    c.measure_all()
+    counts, _, _, _ = oracle.run(c.to_program(), shots=shots, seed=31)
+    assert len(counts) == 16
+    for key in counts:
+        six_sigma(counts[key], shots, 1 / 16)
+    # reset of one half of a Bell pair: that qubit reads 0, the other stays uniform
+    c = C.Circuit(2)
+    c.h(0).cx(0, 1).reset(0).measure(0, 0).measure(1, 1)
+    counts, _, _, _ = oracle.run(c.to_program(), shots=shots, seed=32)
+    assert set(counts) <= {"00", "10"}, counts
+    six_sigma(counts.get("10", 0), shots, 0.5)
+    # a mid-circuit outcome copied forward by CX: both bits always agree
+    c = C.Circuit(2)
+    c.h(0).measure(0, 0).cx(0, 1).measure(1, 1)
+    counts, _, _, _ = oracle.run(c.to_program(), shots=shots, seed=33)
+    assert set(counts) <= {"00", "11"}, counts
+    six_sigma(counts.get("11", 0), shots, 0.5)
+
+
 def test_same_seed_determinism(oracle):
     c = C.random_circuit(6, 8, 3)
     c.measure_all()

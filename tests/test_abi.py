@@ -77,3 +77,26 @@ def test_info_capacity_rows(zc, monkeypatch):
     assert (f64["max_qubits"], f32["max_qubits"]) == (33, 34)
     assert f64["state_bytes"] == 128 << 30 and f64["next_qubit_bytes"] == 256 << 30
     assert info.human(128 << 30) == "128.0 GiB" and info.human(512) == "512 B"
+
+
+def test_noise_model_validated_by_the_abi(zc, monkeypatch):
+    """zc_run validates a non-trivial noise model before anything else, as
+    run_inner does (src/exec.rs:347-351; NoiseModel::validate,
+    src/noise.rs:77-87): every field in [0, 1], NaN rejected, 1 allowed.
+    The Python wrapper's own check is bypassed to reach the C ABI."""
+    from zeno_gb300 import circuit as C
+
+    monkeypatch.setattr(zc.NoiseModel, "validate", lambda self: None)
+    c = C.Circuit(2)
+    c.h(0).cx(0, 1).measure_all()
+    p = c.to_program()
+    for field, bad in (("depolarizing_1q", -0.1), ("depolarizing_1q", 1.5), ("depolarizing_1q", float("nan")),
+                       ("readout_flip_1to0", 1.0001)):
+        with pytest.raises(zc.ZenoCudaError, match=field + r" = .* is not a probability in \[0, 1\]"):
+            zc.run(p, shots=16, seed=1, precision=32, noise=zc.NoiseModel(**{field: bad}))
+    # valid models pass validation (without a GPU the run then fails on the device)
+    for ok in (zc.NoiseModel(depolarizing_1q=1.0), zc.NoiseModel(bit_flip=0.0, phase_flip=0.5)):
+        try:
+            zc.run(p, shots=16, seed=1, precision=32, noise=ok)
+        except zc.ZenoCudaError as e:
+            assert "not a probability" not in str(e)

@@ -14,7 +14,9 @@
 
 #include <algorithm>
 #include <chrono>
+#include <cmath>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "zc_internal.h"
@@ -599,6 +601,26 @@ bool trivial(const zc_noise *m) {
                   m->readout_flip_1to0 == 0.0);
 }
 
+// NoiseModel::validate (src/noise.rs:77-87): every field a probability in
+// [0, 1]; NaN is rejected.
+int validate_noise(const zc_noise &m) {
+    const std::pair<const char *, double> fields[] = {
+        {"depolarizing_1q", m.depolarizing_1q},     {"depolarizing_2q", m.depolarizing_2q},
+        {"bit_flip", m.bit_flip},                   {"phase_flip", m.phase_flip},
+        {"amplitude_damping", m.amplitude_damping}, {"readout_flip_0to1", m.readout_flip_0to1},
+        {"readout_flip_1to0", m.readout_flip_1to0}};
+    for (const auto &f : fields)
+        if (!(f.second >= 0.0 && f.second <= 1.0)) {
+            char buf[128];
+            if (std::isnan(f.second))
+                snprintf(buf, sizeof buf, "%s = NaN is not a probability in [0, 1]", f.first);
+            else
+                snprintf(buf, sizeof buf, "%s = %g is not a probability in [0, 1]", f.first, f.second);
+            return fail(ZC_ERR_INVALID, buf);
+        }
+    return ZC_OK;
+}
+
 // exec_shot_op (src/exec.rs:556-619).
 int shot_op(zc_state *st, const Op &op, const zc_noise *noise, Xoshiro &rng, uint64_t *clbits) {
     if (op.has_if) {
@@ -833,7 +855,12 @@ int zc_run(const zc_program *p, const zc_run_options *opt, zc_run_result *res, u
            size_t cap, double *sv) {
     if (!p || !opt || !res) return fail(ZC_ERR_INVALID, "null argument");
     memset(res, 0, sizeof *res);
+    // run_inner (src/exec.rs:347-351): a non-trivial model is validated first
     const zc_noise *noise = trivial(opt->noise) ? nullptr : opt->noise;
+    if (noise) {
+        const int vrc = validate_noise(*noise);
+        if (vrc) return vrc;
+    }
     if ((noise || p->dynamic) && sv)
         return fail(ZC_ERR_INVALID, noise ? "a noise model is active: the noisy state has no single final state vector"
                                           : "circuit is dynamic: it has no single final state vector");

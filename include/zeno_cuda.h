@@ -97,9 +97,13 @@ const char *zc_last_error(void);
  * Capacity planning retargeted to HBM (src/mem.rs:11-131)              *
  * ------------------------------------------------------------------ */
 
-/* Device memory a state may use: ZENO_MEM_BYTES if set (mem.rs:11-16),
- * else `fraction` of the device's total HBM. */
+/* Device memory a state may use: `fraction` of the device's memory
+ * (mem::budget_bytes without an explicit limit, src/mem.rs:104-111). */
 int zc_device_budget(double fraction, uint64_t *bytes);
+/* The device's memory the budget is taken from (mem::physical_ram_bytes,
+ * src/mem.rs:9-16, retargeted): ZENO_MEM_BYTES if set, pretending to be a
+ * smaller device, else the total HBM. */
+int zc_device_memory(uint64_t *bytes);
 
 /* The current device, for capacity reports (zeno info, src/main.rs:1001-1082
  * with HBM in place of RAM). */

@@ -41,8 +41,15 @@ def test_capacity_planning(zc):
 
 
 def test_env_budget_override(zc, monkeypatch):
+    """ZENO_MEM_BYTES pretends to be a smaller machine (src/mem.rs:9-16); the
+    budget is 0.75 of it: 16 GiB -> 12 GiB -> 29 qubits f64, 30 f32, as
+    tests/cli.rs:126-153 expects of `zeno info`."""
     monkeypatch.setenv("ZENO_MEM_BYTES", str(16 << 30))
-    assert zc.device_budget() == 16 << 30
+    assert zc.device_memory() == 16 << 30
+    budget = zc.device_budget()
+    assert budget == 12 << 30
+    assert zc.max_qubits(budget, 64) == 29 and zc.max_qubits(budget, 32) == 30
+    assert zc.state_bytes(29, 64) == (1 << 29) * 16 and zc.state_bytes(30, 64) == (1 << 30) * 16
 
 
 def _have_gpu():

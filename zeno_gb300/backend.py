@@ -29,7 +29,7 @@ OP_UNITARY, OP_DIAG, OP_CX, OP_MEASURE, OP_RESET, OP_SWAP = 0, 1, 2, 3, 4, 6
 EXPORTS = (
     "zc_create", "zc_create_ex", "zc_destroy", "zc_name", "zc_apply_unitary", "zc_apply_diagonal",
     "zc_apply_cx", "zc_apply_swap", "zc_prob_one", "zc_measure", "zc_reset_all", "zc_sample",
-    "zc_statevector", "zc_norm_sqr", "zc_finish", "zc_last_error", "zc_device_budget", "zc_state_bytes",
+    "zc_statevector", "zc_norm_sqr", "zc_finish", "zc_last_error", "zc_device_budget", "zc_device_memory", "zc_state_bytes",
     "zc_max_qubits", "zc_load_state", "zc_get_stream", "zc_get_counters", "zc_compile", "zc_program_free",
     "zc_program_get_info", "zc_program_get_op", "zc_program_get_final", "zc_run", "zc_profile",
     "zc_profile_read", "zc_sample_noalloc", "zc_set_sweep_shape", "zc_device_info",
@@ -158,6 +158,7 @@ def load() -> C.CDLL:
         "zc_finish": ([vp], i32),
         "zc_last_error": ([], C.c_char_p),
         "zc_device_budget": ([dbl, P(u64)], i32),
+        "zc_device_memory": ([P(u64)], i32),
         "zc_state_bytes": ([u32, i32], u64),
         "zc_max_qubits": ([u64, i32], u32),
         "zc_load_state": ([vp, P(dbl)], i32),
@@ -462,8 +463,16 @@ def device_info() -> Dict[str, object]:
 
 
 def device_budget(fraction: float = 0.75) -> int:
+    """mem::budget_bytes (src/mem.rs:104-111): `fraction` of device_memory()."""
     out = C.c_uint64()
     _check(load().zc_device_budget(fraction, C.byref(out)))
+    return out.value
+
+
+def device_memory() -> int:
+    """mem::physical_ram_bytes for the device: ZENO_MEM_BYTES, else total HBM."""
+    out = C.c_uint64()
+    _check(load().zc_device_memory(C.byref(out)))
     return out.value
 
 

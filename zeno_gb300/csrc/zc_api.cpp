@@ -593,8 +593,9 @@ uint32_t zc_max_qubits(uint64_t budget, int prec) {
     return n;
 }
 
-int zc_device_budget(double fraction, uint64_t *bytes) {
-    if (!bytes) return fail(ZC_ERR_INVALID, "null output");
+// physical_ram_bytes (src/mem.rs:9-16) for the device: ZENO_MEM_BYTES
+// pretends to be a device of that many bytes, else the device's total HBM.
+static int device_memory(uint64_t *bytes) {
     const char *env = getenv("ZENO_MEM_BYTES");
     if (env && *env) {
         char *end = nullptr;
@@ -607,8 +608,23 @@ int zc_device_budget(double fraction, uint64_t *bytes) {
     size_t free_b = 0, total_b = 0;
     cudaError_t e = cudaMemGetInfo(&free_b, &total_b);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemGetInfo");
-    *bytes = (uint64_t)((double)total_b * fraction);
+    *bytes = total_b;
     return ZC_OK;
+}
+
+// budget_bytes without an explicit limit (src/mem.rs:104-111).
+int zc_device_budget(double fraction, uint64_t *bytes) {
+    if (!bytes) return fail(ZC_ERR_INVALID, "null output");
+    uint64_t mem = 0;
+    const int rc = device_memory(&mem);
+    if (rc) return rc;
+    *bytes = (uint64_t)((double)mem * fraction);
+    return ZC_OK;
+}
+
+int zc_device_memory(uint64_t *bytes) {
+    if (!bytes) return fail(ZC_ERR_INVALID, "null output");
+    return device_memory(bytes);
 }
 
 int zc_device_info(zc_device *out) {

@@ -1,6 +1,8 @@
 """Capacity report for the GPU: `zeno info` (src/main.rs:1001-1082) with HBM
-in place of RAM and the device budget of `zc_device_budget` (0.75 x HBM, or
-ZENO_MEM_BYTES).
+in place of RAM: the budget of `zc_device_budget` is 0.75 x the device memory
+(the total HBM, or ZENO_MEM_BYTES pretending to be a smaller device). The
+JSON keeps zeno's schema v1 keys (`ram_bytes` = that device memory, `cores` =
+SMs) and adds the GPU's own.
 
   python -m zeno_gb300.info [--json]
 """
@@ -37,7 +39,8 @@ def capacity(budget: int, precision: int) -> dict:
 def report() -> dict:
     d = zb.device_info()
     budget = zb.device_budget(FRACTION)
-    return {"schema_version": 1, "chip": d["name"], "sms": d["sms"],
+    return {"schema_version": 1, "chip": d["name"], "cores": d["sms"], "ram_bytes": zb.device_memory(),
+            "sms": d["sms"],
             "compute_capability": d["compute_capability"], "hbm_bytes": d["hbm_bytes"],
             "available_now_bytes": d["free_bytes"], "l2_bytes": d["l2_bytes"], "budget_bytes": budget,
             "budget_fraction": FRACTION,
@@ -62,7 +65,7 @@ def main():
         c = r["precisions"][p]
         print("  %-10s %10d %12s %18s" % (p, c["max_qubits"], human(c["state_bytes"]), human(c["next_qubit_bytes"])))
     print()
-    print("ZENO_MEM_BYTES overrides the budget")
+    print("ZENO_MEM_BYTES overrides the device memory the budget is taken from")
 
 
 if __name__ == "__main__":

@@ -559,6 +559,9 @@ int sample_launch_pass2(zc_state *st, const SampleRoute &r, char *d_work, uint64
     const size_t cs_n = r.touched.size() * sizeof(SampleChunk);
     const void *d_us = d_work + out_b, *d_cs = d_work + out_b + us_b;
     int rc = ZC_OK;
+    // Through the ring only when both fit in a quarter of it: if the second
+    // put wraps, the first began past three quarters, beyond the reach of the
+    // second (placed at offset 0), so the kernel reads both intact.
     if (shots * sizeof(double) + cs_n <= st->arena.cap / 4) {
         rc = arena_put(st, r.us.data(), shots * sizeof(double), &d_us);
         if (rc == ZC_OK && cs_n) rc = arena_put(st, r.touched.data(), cs_n, &d_cs);

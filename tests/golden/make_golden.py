@@ -138,14 +138,23 @@ def parse(src):
     return {"n_qubits": sum(s for _, s in qregs), "cregs": cregs, "instrs": instrs}
 
 
-def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+DEFAULT_REF = "/root/reference"
+
+
+def build(ref):
+    """The fixture contents for the examples in the checkout at `ref`."""
     out = {}
     for name in sorted(EXPECTED):
         with open(os.path.join(ref, "examples", name + ".qasm")) as f:
             prog = parse(f.read())
         prog["expected"] = EXPECTED[name]
         out[name] = prog
+    return out
+
+
+def main():
+    ref = sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF
+    out = build(ref)
     with open(os.path.join(HERE, "examples.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)
     print("wrote", os.path.join(HERE, "examples.json"), "with", len(out), "programs")

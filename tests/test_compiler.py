@@ -120,3 +120,26 @@ def test_cancellation_identities(zc, oracle, build, cancelled):
         assert mine.ops == []
     for fusion in (0, 1, 3):
         _same_ops(zc, oracle, p, fusion)
+
+
+@pytest.mark.parametrize("build", [
+    lambda c: c,                                                   # no instructions at all
+    lambda c: c.measure_all(),                                     # measurements only
+    lambda c: c.barrier().barrier(),                               # barriers only
+    lambda c: c.x(0).barrier().x(0).measure_all(),                 # a barrier between a pair
+    lambda c: [c.rz(q, 0.1 * (q + 1)) for q in range(c.n_qubits)] and c,   # one diagonal over every qubit
+    lambda c: [c.cz(q, q + 1) for q in range(c.n_qubits - 1)] and c.cp(0, c.n_qubits - 1, 0.7),
+])
+@pytest.mark.parametrize("n", [1, 12])
+def test_degenerate_programs(zc, oracle, build, n):
+    """Empty, measure-only and barrier-only programs, and diagonal ladders
+    over 12 qubits (wider than the 10-qubit diagonal fusion cap,
+    src/compiler.rs:111-114): same ops as the oracle at every fusion level."""
+    c = C.Circuit(n)
+    try:
+        build(c)
+    except IndexError:
+        pytest.skip("needs two qubits")
+    p = c.to_program()
+    for fusion in (0, 1, 5):
+        _same_ops(zc, oracle, p, fusion)

@@ -49,12 +49,17 @@ int main() {
         std::vector<double> sums(nch, 0.0);
         for (size_t c = 0; c < nch; c++)
             for (size_t i = c * chunk; i < (c + 1) * chunk && i < dim; i++) sums[c] += p2(i);
-        for (uint64_t shots : {1ull, 17ull, 4096ull}) {
+        for (uint64_t shots : {0ull, 1ull, 17ull, 4096ull}) {
             const uint64_t seed = rng();
             std::vector<uint64_t> want(shots), got(shots, ~0ull);
             zo_sample(s, shots, seed, want.data());
             zc::SampleRoute r;
             zc::sample_route(sums.data(), nch, dim, shots, seed, &r);
+            if (r.us.size() != shots || (shots == 0 && !r.touched.empty())) {
+                std::printf("FAIL trial %d: %zu draws, %zu touched chunks for %llu shots\n", trial, r.us.size(),
+                            r.touched.size(), (unsigned long long)shots);
+                return 1;
+            }
             if (r.chunk_len != chunk) {
                 std::printf("FAIL trial %d: chunk length %llu\n", trial, (unsigned long long)r.chunk_len);
                 return 1;

@@ -129,13 +129,17 @@ static bool apply_plan(std::vector<cd> &s, const zc::SweepPlan &plan, int prec, 
 int main() {
     std::mt19937_64 rng(2468);
     std::uniform_real_distribution<double> U(0.0, 2 * M_PI);
-    const uint32_t n = 11;
     double worst[3] = {0, 0, 0};
     size_t sweeps = 0, carried = 0;
-    for (int trial = 0; trial < 240; trial++) {
+    for (int trial = 0; trial < 300; trial++) {
         const int mode = trial % 3;  // 0 exact f64, 1 fast f64 (lowered), 2 fast f32
         const int prec = mode == 2 ? 32 : 64;
         const bool ex = mode == 0;
+        // small tiles (ops on outer qubits, many sweeps), then the kernel's
+        // own shape: 256-byte rows (6 bits f32, 5 bits f64) and 7 high qubits
+        const bool real_shape = trial >= 240;
+        const uint32_t n = real_shape ? 15 : 11;
+        const uint32_t L = real_shape ? (prec == 32 ? 6u : 5u) : 3u, Hcap = real_shape ? 7u : 4u;
         std::vector<QOp> prog;
         const int len = 10 + (int)(rng() % 120);
         for (int i = 0; i < len; i++) {
@@ -183,7 +187,6 @@ int main() {
         std::vector<cd> want = s0, got = s0;
         for (const QOp &op : prog) apply_qop(want, op);
         // the library's flush loop: a sweep from the queue front, or the front op alone
-        const uint32_t L = 3, Hcap = 4;  // small tiles, so ops span several sweeps and outer qubits
         std::vector<QOp> q = prog;
         int guard = 0;
         while (!q.empty()) {

@@ -1,8 +1,9 @@
 """Host logic of the sweep planner (no GPU).
 
-tests/planner_harness.cpp plans random programs on an 11-qubit state sweep by
-sweep through the built library's own plan_sweep / consume_plan (small
-tiles, so ops on outer qubits and carried diagonals occur), decodes each
+tests/planner_harness.cpp plans random programs sweep by sweep through the
+built library's own plan_sweep / consume_plan — on 11 qubits with small
+tiles (ops on outer qubits and carried diagonals occur), and on 15 qubits
+with the kernel's own tile shapes (256-byte rows, 7 high qubits) — decodes each
 sweep's encoded micro-ops through its tile geometry, applies them in
 complex<double> and compares with the program applied directly: identical
 in exact mode (ops kept as given), within 1e-11 for the fast f64 lowering,

@@ -22,7 +22,7 @@ void apply_pass(std::vector<cd> &s, const zc::GroupInfo &q, const std::vector<Op
     if (q.has_dk)
         for (const Op &op : ops)
             if (op.h.kind == zc::MOP_DK && (uint32_t)op.h.table == q.tab_off) dk = &op;
-    for (uint32_t p = 0; p < kSize / E; p++) {
+    for (uint32_t p = 0; p < g_size / E; p++) {
         uint32_t v = p;
         for (int g = 0; g < G; g++) {
             const uint32_t sh = q.sorted[g];
@@ -80,12 +80,14 @@ int main() {
     Gen gen(97531);
     double worst = 0.0;
     size_t passes = 0, folded = 0, fused = 0, translations = 0;
-    for (int trial = 0; trial < 3000; trial++) {
+    for (int trial = 0; trial < 3400; trial++) {
+        // 2^9-element tiles, then the double-float kernel's own 2^12
+        set_tile_bits(trial < 3000 ? 9 : 12);
         gen.new_base();
         const std::vector<Op> ops = gen.list(30);
         std::vector<OpHead> heads;
         for (const Op &op : ops) heads.push_back(op.h);
-        std::vector<cd> s0(kSize);
+        std::vector<cd> s0(g_size);
         for (auto &z : s0) z = cd(gen.U(gen.rng), gen.U(gen.rng));
         std::vector<cd> want = s0;
         for (const Op &op : ops) apply_one(want, op);
@@ -97,7 +99,7 @@ int main() {
             std::vector<zc::GroupInfo> gi(ops.size());
             uint32_t bad = 0;
             int fuse_in = -1, fuse_out = -1;
-            zc::plan_passes(heads.data(), (int)ops.size(), kTileBits, fold, max_group, gi.data(), &bad, &fuse_in,
+            zc::plan_passes(heads.data(), (int)ops.size(), g_tile_bits, fold, max_group, gi.data(), &bad, &fuse_in,
                             &fuse_out);
             if (bad) {
                 std::printf("FAIL trial %d variant %d: planner flagged op %u\n", trial, variant, bad & 0x7fffffffu);

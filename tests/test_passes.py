@@ -1,7 +1,7 @@
 """Register passes of double-float sweeps, checked on the host (no GPU).
 
-tests/passes_harness.cpp plans random micro-op lists on one 2^9-amplitude
-tile with plan_passes (zeno_gb300/csrc/zc_passes.h, the code the sweep kernel
+tests/passes_harness.cpp plans random micro-op lists on one tile (2^9
+amplitudes, and the double-float kernel's own 2^12) with plan_passes (zeno_gb300/csrc/zc_passes.h, the code the sweep kernel
 runs once per job), applies each pass the way the kernel does (the folded CX
 block as an affine load map, the fused table diagonal indexed from the
 descriptor, rows flipped at the store) and compares with the micro-ops applied

@@ -1,6 +1,6 @@
 // Sequential reference for the host checks of the sweep kernel's tile logic
 // (passes_harness.cpp): micro-ops applied one at a time
-// to one tile of 2^kTileBits amplitudes in complex<double>, and a generator
+// to one tile of 2^g_tile_bits amplitudes in complex<double>, and a generator
 // of random micro-op lists shaped like the planner's.
 #pragma once
 #include <cmath>
@@ -16,8 +16,12 @@ namespace tile_ref {
 using cd = std::complex<double>;
 using zc::OpHead;
 
-constexpr uint32_t kTileBits = 9;
-constexpr uint32_t kSize = 1u << kTileBits;
+inline uint32_t g_tile_bits = 9;  // set_tile_bits() changes both
+inline uint32_t g_size = 1u << 9;
+inline void set_tile_bits(uint32_t bits) {
+    g_tile_bits = bits;
+    g_size = 1u << bits;
+}
 constexpr uint32_t kOuter0 = 20, kNOuter = 6;  // outer qubits 20..25
 inline uint64_t g_base = 0;                    // the tile's outer qubit values
 
@@ -32,7 +36,7 @@ inline uint32_t bit_of(uint32_t slot, uint32_t x) {
 }
 
 inline void apply_pair(std::vector<cd> &s, uint32_t a, const cd u[4]) {
-    for (uint32_t i = 0; i < kSize; i++)
+    for (uint32_t i = 0; i < g_size; i++)
         if (!((i >> a) & 1)) {
             const uint32_t j = i | (1u << a);
             const cd x = s[i], y = s[j];
@@ -83,14 +87,14 @@ inline void apply_one(std::vector<cd> &s, const Op &op) {
         }
         case zc::MOP_D1:
         case zc::MOP_DK:
-            for (uint32_t i = 0; i < kSize; i++) s[i] *= diag_entry(op, i);
+            for (uint32_t i = 0; i < g_size; i++) s[i] *= diag_entry(op, i);
             break;
         case zc::MOP_CX:
-            for (uint32_t i = 0; i < kSize; i++)
+            for (uint32_t i = 0; i < g_size; i++)
                 if (bit_of(i, h.a) && !((i >> h.b) & 1)) std::swap(s[i], s[i | (1u << h.b)]);
             break;
         case zc::MOP_SWAP:
-            for (uint32_t i = 0; i < kSize; i++)
+            for (uint32_t i = 0; i < g_size; i++)
                 if (((i >> h.a) & 1) && !((i >> h.b) & 1)) std::swap(s[i], s[(i ^ (1u << h.a)) | (1u << h.b)]);
             break;
     }
@@ -105,7 +109,7 @@ struct Gen {
     std::uniform_real_distribution<double> U{-1.0, 1.0};
     uint32_t tables = 0;
     explicit Gen(uint64_t seed) : rng(seed) {}
-    uint32_t local() { return (uint32_t)(rng() % kTileBits); }
+    uint32_t local() { return (uint32_t)(rng() % g_tile_bits); }
     uint32_t outer() { return zc::kOuterFlag | (kOuter0 + (uint32_t)(rng() % kNOuter)); }
     void new_base() {
         g_base = 0;

@@ -107,3 +107,19 @@ def test_noise_model_validated_by_the_abi(zc, monkeypatch):
             zc.run(p, shots=16, seed=1, precision=32, noise=ok)
         except zc.ZenoCudaError as e:
             assert "not a probability" not in str(e)
+
+
+@pytest.mark.parametrize("lang, std", [("c", "-std=c99"), ("c++", "-std=c++17")])
+def test_headers_compile_as_plain_c_and_cpp(tmp_path, lang, std):
+    """The boundary is a C ABI: both public headers compile alone, warning
+    free and pedantic, as C99 (what a Rust or cgo binding parses) and C++."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc" if lang == "c" else "g++")
+    if cc is None:
+        pytest.skip("no host compiler")
+    src = tmp_path / "hdr.c"
+    src.write_text('#include "zeno_cuda.h"\n#include "zeno_cuda_serve.h"\nint main(void) { return 0; }\n')
+    subprocess.run([cc, std, "-Wall", "-Wextra", "-pedantic", "-Werror", "-x", lang, "-I" + os.path.join(ROOT, "include"),
+                    "-c", str(src), "-o", str(tmp_path / "hdr.o")], check=True)

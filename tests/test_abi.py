@@ -123,3 +123,37 @@ def test_headers_compile_as_plain_c_and_cpp(tmp_path, lang, std):
     src.write_text('#include "zeno_cuda.h"\n#include "zeno_cuda_serve.h"\nint main(void) { return 0; }\n')
     subprocess.run([cc, std, "-Wall", "-Wextra", "-pedantic", "-Werror", "-x", lang, "-I" + os.path.join(ROOT, "include"),
                     "-c", str(src), "-o", str(tmp_path / "hdr.o")], check=True)
+
+
+def test_ctypes_mirrors_match_the_c_layouts(zc, tmp_path):
+    """Every ctypes mirror of a header struct has the C struct's size and each
+    field's C offset (a C program built from the mirrors prints them; a field
+    the C struct lacks fails to compile)."""
+    import ctypes as C
+    import shutil
+    import subprocess
+
+    from zeno_gb300 import serve
+
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no host compiler")
+    pairs = [("zc_device", zc.DeviceC), ("zc_counters", zc.Counters), ("zc_kernel_stat", zc.KernelStat),
+             ("zc_instr", zc.Instr), ("zc_compile_options", zc.CompileOptions), ("zc_op_view", zc.OpView),
+             ("zc_program_info", zc.ProgramInfo), ("zc_noise", zc.NoiseC), ("zc_run_options", zc.RunOptions),
+             ("zc_run_result", zc.RunResultC), ("zc_server_options", serve.ServerOptions),
+             ("zc_server_status", serve.ServerStatus)]
+    lines, want = [], []
+    for cname, py in pairs:
+        lines.append('printf("%%zu\\n", sizeof(%s));' % cname)
+        want.append(C.sizeof(py))
+        for f in py._fields_:
+            lines.append('printf("%%zu\\n", offsetof(%s, %s));' % (cname, f[0]))
+            want.append(getattr(py, f[0]).offset)
+    src = tmp_path / "layout.c"
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "zeno_cuda.h"\n#include "zeno_cuda_serve.h"\n'
+                   "int main(void) {\n" + "\n".join(lines) + "\nreturn 0;\n}\n")
+    exe = str(tmp_path / "layout")
+    subprocess.run([cc, "-std=c99", "-I" + os.path.join(ROOT, "include"), str(src), "-o", exe], check=True)
+    got = [int(x) for x in subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()]
+    assert got == want

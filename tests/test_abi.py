@@ -157,3 +157,17 @@ def test_ctypes_mirrors_match_the_c_layouts(zc, tmp_path):
     subprocess.run([cc, "-std=c99", "-I" + os.path.join(ROOT, "include"), str(src), "-o", exe], check=True)
     got = [int(x) for x in subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split()]
     assert got == want
+
+
+def test_build_targets_sm_103a_only():
+    """Every translation unit is compiled for sm_103a alone (no other
+    architecture, no PTX for JIT), with line info for the profiler, and host
+    code without FMA contraction (bit-identical host arithmetic on x86-64
+    and aarch64)."""
+    from zeno_gb300 import build
+
+    flags = build.NVCC_FLAGS
+    archs = [flags[i + 1] for i, f in enumerate(flags) if f == "-gencode"]
+    assert archs == ["arch=compute_103a,code=sm_103a"]
+    assert "-lineinfo" in flags and "-ffp-contract=off" in flags
+    assert not any(f.startswith(("-arch", "--gpu-architecture")) for f in flags)

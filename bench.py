@@ -3,16 +3,20 @@
 Workload: u3(theta, phi, lambda) with U[0, 2pi) angles on every qubit, then CX
 on a seeded random perfect matching, 40 layers, 30 qubits, f64 split-complex
 state (16 GiB, far larger than L2, so no flush is needed between steps),
-measure all, 1024 shots. One step = one circuit: reset to |0...0>, every
-compiled op, then sampling.
+measure all, 1024 shots, fusion 1. One step = one circuit: reset to
+|0...0>, every compiled op, then sampling.
 
 Prints ONE JSON line (rank 0). `value` = circuits/s with the op stream
-resident on the device side of the API; `e2e` = the same through
-`zc_run` (state allocation, op tables host->device, kernels, sampling,
-indices device->host). `roofline` = the dominant kernel's algorithmic HBM
-bytes per launch over its CUDA-event duration; `cpu_baseline` = the oracle
-(the C restatement of zeno's CPU backend) on all host cores for a bounded
-sample of the same workload.
+resident on the device side of the API, fast arithmetic (double-float on
+the FP32 pipe, f64 storage; within 1e-12 of the FP64 oracle); `e2e` = the
+same through `zc_run` (state allocation, op tables host->device, kernels,
+sampling, indices device->host); `exact_mode` = the same circuit in the
+drop-in's default exact arithmetic (bit-identical to zeno's CPU kernels).
+`roofline` = the dominant kernel's algorithmic HBM bytes per launch over its
+CUDA-event duration; `cpu_baseline` = the oracle (the C restatement of
+zeno's CPU backend) on all host cores for a bounded sample of the same
+workload. `configs` = every other seeded workload at its own shape
+(zeno_gb300/workloads.py).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 """
@@ -31,7 +35,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-HBM_FALLBACK_GBS = 6800.0
+METRIC = "30q circuit throughput (u3 + matching-CX, depth 40, f64)"
 # DRAM read+write per launch over algorithmic bytes, from an ncu capture of
 # the f64 double-float sweep kernel at 26 qubits (state 8x the L2):
 # 1.074 GB read + 1.027 GB write against 2S = 2.147 GB.
@@ -49,7 +53,7 @@ SWEEP_DF_PIPES = {"issue_active_pct": 57.6, "fma_pipe_pct": 36.5, "alu_pipe_pct"
 # data only.
 DF_FP32_INSTR_PER_AMP = {"complex": 86, "diag1": 38, "diag_table": 32, "cx": 0, "swap": 0, "real": 38,
                          "rotation": 24}
-FP32_INSTR_PEAK = 34.3e12  # measured FMA issue rate (zeno_gb300/probes/fp_peaks.cu)
+CONFIG_NAMES = ("matching_20q", "qft", "fusion_sweep", "big_state", "trajectories", "gate_mix_tc", "serving")
 
 
 def parse():
@@ -66,29 +70,33 @@ def parse():
     ap.add_argument("--shots", type=int, default=1024)
     ap.add_argument("--seed", type=int, default=7)
     ap.add_argument("--cpu-layers", type=int, default=1, help="layers timed for the CPU baseline sample")
+    ap.add_argument("--validate-qubits", type=int, default=24,
+                    help="reference arm: full circuit timed at this size against its per-layer projection")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-exact", action="store_true", help="skip the exact-mode circuit")
     ap.add_argument("--no-check", action="store_true", help="skip the fast-vs-exact accuracy check")
     ap.add_argument("--check-qubits", type=int, default=26)
-    ap.add_argument("--no-extras", action="store_true", help="skip the batched-trajectory measurement")
+    ap.add_argument("--configs", default="all",
+                    help="comma list of %s, 'all' or 'none'" % ",".join(CONFIG_NAMES))
     return ap.parse_args()
 
 
-def peaks():
-    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
-    try:
-        with open(path) as f:
-            d = json.load(f)
-        return float(d["hbm_gbs"]), "measured"
-    except Exception:
-        return HBM_FALLBACK_GBS, "fallback"
+def headline_config(a):
+    """The workload, identical in both arms' lines (the arithmetic is reported
+    beside it, under `arithmetic`)."""
+    S = (1 << a.qubits) * (a.precision // 8) * 2
+    return {"workload": "%dq depth-%d u3+matching-CX f%d, %d shots, fusion %d" % (
+        a.qubits, a.depth, a.precision, a.shots, a.fusion),
+        "l2": "state %.0f GiB > 129 MB L2: no flush needed" % (S / 2**30)}
 
 
-def workload_name(a):
-    arith = {"exact": "exact (reference expression trees, native FP)",
-             "fast": "fast (double-float on the FP32 pipe, f64 storage)" if a.precision == 64 else "fast (FMA)"}
-    return "%dq depth-%d u3+matching-CX f%d, %d shots, fusion %d, %s arithmetic" % (
-        a.qubits, a.depth, a.precision, a.shots, a.fusion, arith[a.mode])
+def arithmetic_name(mode, precision):
+    if mode == "exact":
+        return "exact: zeno's expression trees, separately rounded, no FMA (bit-identical to its CPU kernels)"
+    if precision == 64:
+        return "fast: double-float (FP32 pairs) on the FP32 pipe, f64 storage; within 1e-12 of the FP64 oracle"
+    return "fast: FMA-contracted f32; within 1e-5 of the FP64 oracle"
 
 
 def accuracy_check(a, zc, C):
@@ -104,44 +112,6 @@ def accuracy_check(a, zc, C):
     return {"qubits": a.check_qubits, "depth": a.depth, "max_abs_damp": d, "tvd": tvd,
             "reference": "exact mode (bit-identical to the FP64 oracle in the parity tests)",
             "tolerance": {"max_abs_damp": 1e-12 if a.precision == 64 else 1e-5, "tvd": 1e-6}}
-
-
-def batched_trajectories(zc, C):
-    """16 qubits, depth 20, depolarizing 1e-3 (1q) / 1e-2 (CX), damping 1e-3,
-    2% readout, 4096 trajectories in one launch vs the per-shot replay."""
-    noise = zc.NoiseModel(depolarizing_1q=1e-3, depolarizing_2q=1e-2, amplitude_damping=1e-3,
-                          readout_flip_0to1=0.02, readout_flip_1to0=0.02)
-    p = C.matching_circuit(16, 20, 7).to_program()
-    prog = zc.compile(p, 0)
-    zc.run(p, shots=256, seed=1, precision=32, noise=noise, program=prog)
-    t0 = time.perf_counter()
-    r = zc.run(p, shots=4096, seed=2, precision=32, noise=noise, program=prog)
-    tb = time.perf_counter() - t0
-    plain_shots = 32
-    t0 = time.perf_counter()
-    zc.run(p, shots=plain_shots, seed=2, precision=32, noise=noise, program=prog, flags=zc.FLAG_PER_SHOT)
-    tp = (time.perf_counter() - t0) / plain_shots
-    return {"workload": "16q depth-20 u3+matching-CX f32, dep 1e-3/1e-2, damping 1e-3, readout 2%, 4096 trajectories",
-            "trajectories_per_s": 4096 / tb, "seconds": tb, "launches": r.launches, "batched": r.batched,
-            "plain_per_shot_trajectories_per_s": 1.0 / tp, "plain_sample_shots": plain_shots,
-            "speedup_vs_plain": (4096 / tb) * tp}
-
-
-def serving_sample(zc):
-    """A short request stream (8..22 qubits, gate-mix circuits, Poisson
-    arrivals at 3000 req/s): the continuous-batching server against one
-    circuit per call in arrival order."""
-    from zeno_gb300 import serve
-
-    reqs = serve.request_stream(300, rate=3000.0, master_seed=2024, n_max=22)
-    serve.compile_requests(reqs)
-    s = serve.serve_stream(reqs)
-    plain = serve.request_stream(300, rate=3000.0, master_seed=2024, n_max=22)
-    for a, b in zip(plain, reqs):
-        a.program = b.program
-    pl = serve.plain_stream(plain)
-    return {"workload": "300 requests, 8..22 qubits, depth U[4,60], shots 1..8192, Poisson 3000 req/s, 5% f64",
-            "server": s, "one_per_call": pl, "throughput_ratio": s["circuits_per_s"] / pl["circuits_per_s"]}
 
 
 class Clocks:
@@ -194,16 +164,44 @@ class Clocks:
                 "reasons": reasons, "samples": len(rows)}
 
 
-def cpu_baseline(a, threads=None):
-    """The oracle on the host cores for a bounded sample: state allocation,
-    `cpu_layers` layers of the circuit and the sampler, scaled to one circuit."""
+# ---------------------------------------------------------------- CPU legs
+# (the oracle is loaded only here: the CPU baseline of our line and the
+# reference arm)
+
+
+def _oracle(threads=None):
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
-    from zeno_gb300 import circuit as C
-
     oracle.build()
     oracle.set_threads(threads or os.cpu_count() or 1)
+    return oracle
+
+
+def layer_programs(a, qubits):
+    """The headline circuit cut into its `depth` layers (n u3 + n/2 CX each),
+    each compiled with the oracle's compiler at the headline's fusion. For
+    this circuit nothing fuses across a layer boundary (a CX on every qubit
+    separates one layer's u3 from the next), so the layers' ops are the whole
+    circuit's ops."""
+    from zeno_gb300 import circuit as C
+
+    oracle = _oracle()
+    p = C.matching_circuit(qubits, a.depth, a.seed, measure=False).to_program()
+    per = len(p.instrs) // a.depth
+    out = []
+    for layer in range(a.depth):
+        lp = C.Program(qubits, [], p.instrs[layer * per:(layer + 1) * per])
+        out.append(oracle.compile(lp, a.fusion))
+    return out
+
+
+def cpu_baseline(a, threads=None):
+    """The oracle on the host cores for a bounded sample: state allocation,
+    `cpu_layers` layers of the circuit and the sampler, scaled to one circuit."""
+    from zeno_gb300 import circuit as C
+
+    oracle = _oracle(threads)
     nthreads = oracle.threads()
     layer = C.matching_circuit(a.qubits, a.cpu_layers, a.seed, measure=False).to_program()
     comp = oracle.compile(layer, a.fusion)
@@ -224,6 +222,110 @@ def cpu_baseline(a, threads=None):
                                               a.depth // a.cpu_layers),
         "seconds_sampled": t3 - t0,
     }
+
+
+def cpu_trajectories(shots=256):
+    """The oracle's per-shot noisy path (zeno's run_per_shot, parallel over
+    shots on every host core) on the trajectory workload: 16 qubits, depth
+    20, f32, the same noise model; a bounded sample of `shots` trajectories."""
+    from zeno_gb300 import circuit as C
+    from zeno_gb300 import workloads as W
+
+    oracle = _oracle()
+
+    class _Noise:
+        pass
+
+    nz = _Noise()
+    for f, _ in oracle.ZoNoise._fields_:
+        setattr(nz, f, 0.0)
+    for k, v in W.TRAJ_NOISE.items():
+        setattr(nz, k, v)
+    p = C.matching_circuit(16, 20, 7).to_program()
+    t0 = time.perf_counter()
+    oracle.run(p, prec=32, shots=shots, seed=2, noise=nz)
+    t = time.perf_counter() - t0
+    return {"value": shots / t, "unit": "trajectories/s", "cores": oracle.threads(), "kind": "port",
+            "sample": "%d trajectories of the same workload (per-shot replay, parallel over shots)" % shots,
+            "seconds_sampled": t}
+
+
+def reference_arm(a):
+    """zeno's CPU backend (the oracle port, all host threads) on the headline
+    circuit. A step is one layer of the circuit applied to a persistent 30q
+    state (40 consecutive steps are one whole circuit); state allocation, the
+    first layer and the 1024-shot sampling are timed once. value = 1 circuit /
+    (allocation + first layer + 39 x mean later layer + sampling).
+    Validation: the whole 40-layer circuit timed at `validate_qubits` against
+    the same projection."""
+    rank, ws, _ = dist_init(a)
+    if rank != 0:
+        return
+    oracle = _oracle()
+    nthreads = oracle.threads()
+
+    def project(qubits, steps, warmup):
+        layers = layer_programs(a, qubits)
+        t0 = time.perf_counter()
+        st = oracle.State(qubits, a.precision)
+        t_alloc = time.perf_counter() - t0
+        ts_all = []
+        for i in range(warmup + steps):
+            c = layers[i % a.depth]
+            t0 = time.perf_counter()
+            for op in c.ops:
+                st.apply_op(op)
+            ts_all.append(time.perf_counter() - t0)
+        t0 = time.perf_counter()
+        st.sample(a.shots, 1)
+        t_sample = time.perf_counter() - t0
+        st.close()
+        # the first layer also pays the first touch of the zeroed pages
+        # (zeno's zero_state is a calloc too); it is timed, not projected
+        ts = ts_all[max(1, warmup):]
+        layer_s = statistics.mean(ts)
+        circuit = t_alloc + ts_all[0] + (a.depth - 1) * layer_s + t_sample
+        return t_alloc, ts_all[0], layer_s, t_sample, ts, layers, circuit
+
+    # validation at a smaller size: full circuit vs projection
+    _, _, _, _, _, layers_v, proj_v = project(a.validate_qubits, 3, 1)
+    t0 = time.perf_counter()
+    st = oracle.State(a.validate_qubits, a.precision)
+    for c in layers_v:
+        for op in c.ops:
+            st.apply_op(op)
+    st.sample(a.shots, 1)
+    full_v = time.perf_counter() - t0
+    st.close()
+
+    t_alloc, first_s, layer_s, t_sample, ts, _, per_circuit = project(a.qubits, a.steps, a.warmup)
+    v = 1.0 / per_circuit
+    sample = ("one layer (%d u3 + %d CX) of the %d-layer circuit per step on a persistent %dq state, %d threads; "
+              "allocation, the first layer (first touch of the zeroed state) and %d-shot sampling timed once; "
+              "circuit = allocation + first layer + %d x mean later layer + sampling"
+              % (a.qubits, a.qubits // 2, a.depth, a.qubits, nthreads, a.shots, a.depth - 1))
+    line = {
+        "impl": "reference", "metric": METRIC,
+        "value": v, "unit": "circuits/s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": statistics.mean(ts) * 1000.0, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64" if a.precision == 64 else "f32",
+        "data": "synthetic (seeded circuit, random angles)",
+        "config": headline_config(a),
+        "arithmetic": arithmetic_name("exact", a.precision),
+        "cpu_baseline": {"kind": "port", "cores": nthreads, "sample": sample, "value": v, "unit": "circuits/s"},
+        "e2e": {"value": v, "unit": "circuits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "step_unit": "one circuit layer (1/%d of a circuit)" % a.depth,
+        "extrapolated": True,
+        "measured": {"layers_timed": len(ts), "layer_seconds_mean": layer_s,
+                     "layer_seconds_min": min(ts), "layer_seconds_max": max(ts),
+                     "allocation_seconds": t_alloc, "first_layer_seconds": first_s,
+                     "sampling_seconds": t_sample,
+                     "circuit_seconds_projected": per_circuit},
+        "validation": {"qubits": a.validate_qubits, "full_circuit_seconds": full_v,
+                       "projected_seconds": proj_v, "projected_over_full": proj_v / full_v},
+        "note": "C restatement of zeno's scalar CPU backend (the Rust binary cannot be built here)",
+    }
+    print(json.dumps(line), flush=True)
 
 
 def dist_init(a):
@@ -258,28 +360,31 @@ def job_throughput(units_per_rank, seconds, ws):
     return units_per_rank * ws / seconds, seconds
 
 
-def reference_arm(a):
-    rank, ws, _ = dist_init(a)
-    if rank != 0:
-        return
-    steps = []
-    for i in range(a.warmup + a.steps):
-        r = cpu_baseline(a)
-        if i >= a.warmup:
-            steps.append(r)
-    v = statistics.median(s["value"] for s in steps)
-    line = {
-        "impl": "reference", "metric": "30q circuit throughput (u3 + matching-CX, depth 40, f64)",
-        "value": v, "unit": "circuits/s", "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
-        "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if a.precision == 64 else "f32", "data": "synthetic (seeded circuit)",
-        "config": {"workload": workload_name(a), "l2": "state 16 GiB > L2, no flush needed"},
-        "cpu_baseline": {k: steps[-1][k] for k in ("kind", "cores", "sample")} | {"value": v,
-                                                                                 "unit": "circuits/s"},
-        "e2e": {"value": v, "unit": "circuits/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "note": "C restatement of zeno's scalar CPU backend (the Rust binary cannot be built here)",
-    }
-    print(json.dumps(line), flush=True)
+def run_configs(a, peak, pk, line):
+    from zeno_gb300 import workloads as W
+
+    want = CONFIG_NAMES if a.configs == "all" else () if a.configs == "none" else tuple(
+        x for x in a.configs.split(",") if x)
+    out = {}
+    for name in want:
+        t0 = time.perf_counter()
+        try:
+            if name == "gate_mix_tc":
+                out[name] = W.gate_mix_tc(peak, pk.get("tf32_tflops"))
+            else:
+                out[name] = getattr(W, name)(peak)
+        except Exception as e:  # one failing workload must not hide the others
+            out[name] = {"error": "%s: %s" % (type(e).__name__, e)}
+        if isinstance(out[name], dict):
+            out[name]["bench_wall_s"] = time.perf_counter() - t0
+        else:
+            out[name] = {"rows": out[name], "bench_wall_s": time.perf_counter() - t0}
+    if "trajectories" in out and not a.no_cpu:
+        out["trajectories"]["cpu_baseline"] = cpu_trajectories()
+        t = out["trajectories"]
+        if "trajectories_per_s" in t:
+            t["speedup_vs_cpu_baseline"] = t["trajectories_per_s"] / t["cpu_baseline"]["value"]
+    line["configs"] = out
 
 
 def main():
@@ -292,6 +397,7 @@ def main():
     from zeno_gb300 import backend as zc
     from zeno_gb300 import build as zb
     from zeno_gb300 import circuit as C
+    from zeno_gb300 import peaks
     from zeno_gb300.rng import splitmix64
 
     if rank == 0:
@@ -305,9 +411,10 @@ def main():
     circ = C.matching_circuit(a.qubits, a.depth, a.seed).to_program()
     prog = zc.compile(circ, a.fusion)
     ops = prog.ops
+    pk = peaks.measure(with_tf32=rank == 0 and a.configs != "none")
+    peak, peak_kind = pk["hbm_gbs"], pk["hbm_source"]
     be = zc.CudaBackend(a.qubits, a.precision, flags)
     stream = torch.cuda.ExternalStream(be.stream())
-    S = (1 << a.qubits) * (a.precision // 8) * 2
     sample_seed = splitmix64(a.seed)
 
     def step():
@@ -352,17 +459,18 @@ def main():
     fp32_instr = sum(n * DF_FP32_INSTR_PER_AMP[k] for k, n in mops.items()) * float(1 << a.qubits)
     dom = max(classes, key=lambda c: classes[c]["ms"])
     dd = classes[dom]
-    peak, peak_kind = peaks()
     achieved = (dd["bytes"] / dd["launches"]) / (dd["ms"] / dd["launches"] / 1000.0) / 1e9
+    df_sweep = dom == "sweep" and a.mode == "fast" and a.precision == 64
     line = {
-        "metric": "30q circuit throughput (u3 + matching-CX, depth 40, f64)",
+        "metric": METRIC,
         "value": value, "unit": "circuits/s", "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": elapsed / a.steps * 1000.0, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64" if a.precision == 64 else "f32",
         "data": "synthetic (seeded circuit, random angles)",
-        "config": {"workload": workload_name(a), "parallelism": "replicas" if ws > 1 else "single",
-                   "l2": "state %.0f GiB > 129 MB L2: no flush needed" % (S / 2**30),
-                   "ops": len(ops), "input_gates": prog.stats["input_gates"]},
+        "config": headline_config(a),
+        "arithmetic": arithmetic_name(a.mode, a.precision),
+        "parallelism": "replicas" if ws > 1 else "single",
+        "ops": len(ops), "input_gates": prog.stats["input_gates"],
         "gpu_launches": int(c1["launches"] - c0["launches"]),
         "gpu_busy_frac": gates_ms / 1000.0 / elapsed,
         "amp_updates_per_s": {"value": prog.stats["input_gates"] * 2.0 ** a.qubits * value,
@@ -379,23 +487,22 @@ def main():
                                  if dom in MEASURED_TRAFFIC_RATIO else None),
                      "ops_per_launch": len(ops) * a.steps / dd["launches"] if dom == "sweep" else 1.0,
                      "limiter": ("FP32/ALU issue: each sweep applies many gates per HBM pass in double-float "
-                                 "arithmetic; ncu at 26q: %s" % SWEEP_DF_PIPES)
-                     if dom == "sweep" and a.mode == "fast" and a.precision == 64 else None,
+                                 "arithmetic; ncu at 26q: %s" % SWEEP_DF_PIPES) if df_sweep else None,
                      "compute": ({"bound": "fp32_pipe", "unit": "FP32 instr/s",
                                   "achieved": fp32_instr / (dd["ms"] / 1e3),
-                                  "peak": FP32_INSTR_PEAK,
-                                  "frac": fp32_instr / (dd["ms"] / 1e3) / FP32_INSTR_PEAK,
+                                  "peak": pk["fp32_fma_per_s"], "peak_source": "measured live (zc_measure_arith_peaks)",
+                                  "frac": fp32_instr / (dd["ms"] / 1e3) / pk["fp32_fma_per_s"],
                                   "micro_ops": mops,
                                   "count": "sweep micro-ops issued in the timed steps x FP32 instructions per "
                                            "amplitude of their double-float arithmetic %s; index arithmetic, "
                                            "data moves and f64 <-> double-float conversions not counted"
-                                           % DF_FP32_INSTR_PER_AMP})
-                     if dom == "sweep" and a.mode == "fast" and a.precision == 64 else None},
+                                           % DF_FP32_INSTR_PER_AMP}) if df_sweep else None},
+        "peaks": pk,
         "clocks": clk.summary(),
     }
+    torch.cuda.synchronize()
+    be.close()
     if not a.no_e2e:
-        torch.cuda.synchronize()
-        be.close()
         h2d = 0
         for op in ops:
             if op.kind in (zc.OP_UNITARY, zc.OP_DIAG):
@@ -412,11 +519,21 @@ def main():
         line["e2e"] = {"value": e2e_value, "unit": "circuits/s", "h2d_bytes_per_step": h2d,
                        "d2h_bytes_per_step": d2h, "sim_seconds": r.sim_time,
                        "path": "zc_run: allocate state, per-op host->device tables, kernels, sample, read indices"}
-    if rank == 0 and not a.no_extras:
-        line["batched_trajectories"] = batched_trajectories(zc, C)
-        line["serving"] = serving_sample(zc)
+    if rank == 0 and a.mode == "fast" and not a.no_exact:
+        # the drop-in's default (zc_create): exact arithmetic, one whole circuit
+        t0 = time.perf_counter()
+        r = zc.run(circ, shots=a.shots, seed=a.seed, precision=a.precision, flags=zc.FLAG_EXACT, program=prog)
+        t = time.perf_counter() - t0
+        line["exact_mode"] = {"workload": headline_config(a)["workload"], "arithmetic": arithmetic_name("exact", 64),
+                              "seconds": t, "circuits_per_s": 1.0 / t, "sim_seconds": r.sim_time,
+                              "sweeps": r.sweeps, "launches": r.launches,
+                              "pass_GBps": r.bytes_moved / t / 1e9, "roofline_frac": r.bytes_moved / t / 1e9 / peak,
+                              "fp64_fma_per_s_peak": pk["fp64_fma_per_s"],
+                              "path": "zc_run through the drop-in's default arithmetic (ZC_FLAG_EXACT)"}
     if rank == 0 and a.mode == "fast" and not a.no_check:
         line["accuracy"] = accuracy_check(a, zc, C)
+    if rank == 0 and a.configs != "none":
+        run_configs(a, peak, pk, line)
     if rank == 0 and not a.no_cpu:
         line["cpu_baseline"] = cpu_baseline(a)
     if rank == 0:

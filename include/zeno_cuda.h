@@ -140,6 +140,18 @@ int zc_get_counters(zc_state *st, zc_counters *out);
  * Used by the autotuner (zeno_gb300/autotune.py); results do not depend on it. */
 int zc_set_sweep_shape(zc_state *st, uint32_t max_high);
 
+/* Arithmetic issue rates of the current device, measured by timing
+ * issue-bound FMA loops (no counterpart in the reference): the compute
+ * denominators of the rooflines the benchmarks report beside HBM GB/s
+ * (double-float f64 sweeps run on the FP32 pipe, exact f64 on the FP64
+ * pipe). Rates are FMA operations per second over the whole device. */
+typedef struct {
+    double fp64_fma_per_s;
+    double fp32_fma_per_s;
+    uint32_t sms, _pad;
+} zc_arith_peaks;
+int zc_measure_arith_peaks(zc_arith_peaks *out);
+
 /* Per-launch profiling: with profiling on, every kernel launch of this
  * state is bracketed by CUDA events on its stream. zc_profile(st, 1)
  * starts (and clears) a recording, zc_profile_read flushes, synchronises

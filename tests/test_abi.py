@@ -142,7 +142,7 @@ def test_ctypes_mirrors_match_the_c_layouts(zc, tmp_path):
              ("zc_instr", zc.Instr), ("zc_compile_options", zc.CompileOptions), ("zc_op_view", zc.OpView),
              ("zc_program_info", zc.ProgramInfo), ("zc_noise", zc.NoiseC), ("zc_run_options", zc.RunOptions),
              ("zc_run_result", zc.RunResultC), ("zc_server_options", serve.ServerOptions),
-             ("zc_server_status", serve.ServerStatus)]
+             ("zc_server_status", serve.ServerStatus), ("zc_arith_peaks", zc.ArithPeaksC)]
     lines, want = [], []
     for cname, py in pairs:
         lines.append('printf("%%zu\\n", sizeof(%s));' % cname)

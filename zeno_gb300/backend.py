@@ -32,7 +32,7 @@ EXPORTS = (
     "zc_statevector", "zc_norm_sqr", "zc_finish", "zc_last_error", "zc_device_budget", "zc_device_memory", "zc_state_bytes",
     "zc_max_qubits", "zc_load_state", "zc_get_stream", "zc_get_counters", "zc_compile", "zc_program_free",
     "zc_program_get_info", "zc_program_get_op", "zc_program_get_final", "zc_run", "zc_profile",
-    "zc_profile_read", "zc_sample_noalloc", "zc_set_sweep_shape", "zc_device_info",
+    "zc_profile_read", "zc_sample_noalloc", "zc_set_sweep_shape", "zc_device_info", "zc_measure_arith_peaks",
 )
 
 
@@ -40,6 +40,11 @@ class DeviceC(C.Structure):
     _fields_ = [("name", C.c_char * 64), ("sms", C.c_uint32), ("cc_major", C.c_uint32), ("cc_minor", C.c_uint32),
                 ("_pad", C.c_uint32), ("hbm_bytes", C.c_uint64), ("free_bytes", C.c_uint64),
                 ("l2_bytes", C.c_uint64)]
+
+
+class ArithPeaksC(C.Structure):
+    _fields_ = [("fp64_fma_per_s", C.c_double), ("fp32_fma_per_s", C.c_double), ("sms", C.c_uint32),
+                ("_pad", C.c_uint32)]
 
 
 class ZenoCudaError(RuntimeError):
@@ -175,6 +180,7 @@ def load() -> C.CDLL:
         "zc_profile_read": ([vp, P(KernelStat), i32, P(i32)], i32),
         "zc_set_sweep_shape": ([vp, u32], i32),
         "zc_device_info": ([P(DeviceC)], i32),
+        "zc_measure_arith_peaks": ([P(ArithPeaksC)], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -460,6 +466,14 @@ def device_info() -> Dict[str, object]:
     _check(load().zc_device_info(C.byref(d)))
     return {"name": d.name.decode(), "sms": d.sms, "compute_capability": "%d.%d" % (d.cc_major, d.cc_minor),
             "hbm_bytes": d.hbm_bytes, "free_bytes": d.free_bytes, "l2_bytes": d.l2_bytes}
+
+
+def arith_peaks() -> Dict[str, float]:
+    """FP64 / FP32 FMA issue rates of the current device (operations per
+    second over the whole GPU), timed on issue-bound FMA loops."""
+    d = ArithPeaksC()
+    _check(load().zc_measure_arith_peaks(C.byref(d)))
+    return {"fp64_fma_per_s": d.fp64_fma_per_s, "fp32_fma_per_s": d.fp32_fma_per_s, "sms": d.sms}
 
 
 def device_budget(fraction: float = 0.75) -> int:

@@ -6,14 +6,14 @@
 Per state size, precision and arithmetic mode: one-qubit gate passes on
 low and high qubits, CX, a 3-qubit diagonal, dense k-qubit blocks, a sweep
 of 1/4/7 one-qubit gates, sampling and prob_one; each reported as time and
-algorithmic GB/s (2S per pass, S for CX). `--fp-peaks` compiles and runs
-probes/fp_peaks.cu (FP64 and FP32 instruction rates). `--sweep-costs N`
+algorithmic GB/s (2S per pass, S for CX). `--fp-peaks` prints the FP64 /
+FP32 FMA issue rates and the TF32 GEMM rate (zeno_gb300/peaks.py). `--sweep-costs N`
 prints the cost of one micro-op of each kind inside a sweep.
 """
 
 import argparse
+import json
 import os
-import subprocess
 import sys
 
 import numpy as np
@@ -22,13 +22,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 
 def fp_peaks():
-    from .build import ARCH, nvcc
+    from . import peaks
 
-    src = os.path.join(HERE, "probes", "fp_peaks.cu")
-    exe = os.path.join(HERE, "_lib", "fp_peaks")
-    os.makedirs(os.path.dirname(exe), exist_ok=True)
-    subprocess.run([nvcc()] + ARCH + ["-O3", "-o", exe, src], check=True)
-    print(subprocess.run([exe], check=True, capture_output=True, text=True).stdout, end="")
+    print(json.dumps(peaks.measure()))
 
 
 def timed(be, torch, fn, reps=3):

@@ -1,0 +1,291 @@
+"""Measurement drivers for the five seeded workloads the backend is judged on.
+
+Each function runs one workload at its own shape on the current GPU and
+returns a JSON-ready dict: seconds (wall-clock around complete `zc_run`
+calls: state allocation, ops, sampling, indices back to the host — zeno's
+sim_time semantics, src/exec.rs:372-381), device time per kernel class from
+the in-library CUDA-event profiler, algorithmic HBM GB/s and its fraction of
+the measured copy peak, and the accuracy against an f64 run where the
+workload states one.
+
+  * `matching_20q`   20 qubits, depth 12, u3 + matching CX, f64, 1024 shots
+  * `qft`            QFT 24 / 28 qubits, f64 / f32, exact / fast, 8192 shots
+  * `fusion_sweep`   30 qubits, depth 40, f64 fast, fusion widths K = 1..5
+  * `big_state`      33 qubits, depth 40, f64 fast (128 GiB)
+  * `trajectories`   4096 noisy 16-qubit trajectories (f32), one launch
+  * `gate_mix_tc`    28 qubits, depth 60 gate mix: f32 sweeps and 3xTF32
+                     tensor-core blocks (k = 5, 6, 7) against f64
+  * `serving`        10,000-request stream (8..26 qubits) at several arrival
+                     rates: continuous batching against one circuit per call
+
+Algorithmic bytes: one pass over the state reads and writes it once (2S,
+S = 2^n x 2 x bytes per real); a standalone CX or SWAP moves S; a multi-op
+sweep counts 2S once.
+"""
+
+from __future__ import annotations
+
+import statistics
+import time
+from typing import Dict, List, Optional
+
+import numpy as np
+
+from . import backend as zb
+from . import circuit as C
+from .rng import splitmix64
+
+
+def _apply(be, prog):
+    for op in prog.ops:
+        if op.kind == zb.OP_UNITARY:
+            be.apply_unitary(op.qubits, op.data)
+        elif op.kind == zb.OP_DIAG:
+            be.apply_diagonal(op.qubits, op.data)
+        elif op.kind == zb.OP_CX:
+            be.apply_cx(op.a, op.b)
+        elif op.kind == zb.OP_SWAP:
+            be.apply_swap(op.a, op.b)
+
+
+def _timed_runs(p, prog, prec, flags, shots, seed, reps):
+    """Median wall seconds of `reps` complete zc_run calls (after one warm-up)."""
+    zb.run(p, shots=shots, seed=seed, precision=prec, flags=flags, program=prog)
+    ts, r = [], None
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        r = zb.run(p, shots=shots, seed=seed, precision=prec, flags=flags, program=prog)
+        ts.append(time.perf_counter() - t0)
+    return statistics.median(ts), r
+
+
+def device_profile(n, prec, flags, prog, shots, seed, peak_gbs) -> Dict[str, object]:
+    """One circuit on a CudaBackend with per-launch CUDA events: every kernel
+    class's launches, time and algorithmic bytes; the dominant class's
+    achieved GB/s against the copy peak."""
+    be = zb.CudaBackend(n, prec, flags)
+    try:
+        _apply(be, prog)  # warm-up: first-launch costs stay out of the record
+        be.sample(shots, seed)
+        be.reset_all()
+        be.finish()
+        be.profile(True)
+        _apply(be, prog)
+        be.sample(shots, seed)
+        prof = be.profile_read()
+        be.profile(False)
+    finally:
+        be.close()
+    dev_ms = sum(d["ms"] for d in prof.values())
+    dom = max(prof, key=lambda c: prof[c]["ms"]) if prof else None
+    out = {"device_ms": dev_ms,
+           "kernels": {c: {"launches": d["launches"], "ms": round(d["ms"], 3),
+                           "GBps": round(d["bytes"] / (d["ms"] * 1e-3) / 1e9, 1) if d["ms"] and d["bytes"] else None}
+                       for c, d in sorted(prof.items())}}
+    if dom is not None and prof[dom]["bytes"]:
+        ach = prof[dom]["bytes"] / (prof[dom]["ms"] * 1e-3) / 1e9
+        out["roofline"] = {"kernel": dom, "bound": "hbm", "achieved_GBps": ach, "peak_GBps": peak_gbs,
+                           "frac": ach / peak_gbs, "share_of_device_time": prof[dom]["ms"] / dev_ms}
+    return out
+
+
+def _accuracy(a: np.ndarray, ref: np.ndarray) -> Dict[str, float]:
+    return {"max_abs_damp": float(np.abs(a - ref).max()),
+            "tvd": float(0.5 * np.abs(np.abs(a) ** 2 - np.abs(ref) ** 2).sum())}
+
+
+def matching_20q(peak_gbs) -> Dict[str, object]:
+    """20 qubits, depth 12: u3 with U[0, 2pi) angles on every qubit, then CX
+    on a seeded random perfect matching; f64, measure all, 1024 shots,
+    fusion 1 (zeno's default)."""
+    n, depth, shots, seed = 20, 12, 1024, 7
+    p = C.matching_circuit(n, depth, seed).to_program()
+    prog = zb.compile(p, 1)
+    out = {"workload": "20q depth-12 u3+matching-CX f64, 1024 shots, fusion 1", "ops": len(prog.ops),
+           "input_gates": prog.stats["input_gates"]}
+    for mode, flags in (("exact", zb.FLAG_EXACT), ("fast", zb.FLAG_FAST)):
+        t, r = _timed_runs(p, prog, 64, flags, shots, seed, 5)
+        d = device_profile(n, 64, flags, prog, shots, splitmix64(seed), peak_gbs)
+        out[mode] = {"seconds": t, "circuits_per_s": 1.0 / t, "sweeps": r.sweeps, "launches": r.launches,
+                     "amp_updates_per_s": prog.stats["input_gates"] * 2.0 ** n / t, **d}
+    ex = zb.run(p, shots=0, precision=64, flags=zb.FLAG_EXACT, statevector=True, program=prog).statevector
+    fa = zb.run(p, shots=0, precision=64, flags=zb.FLAG_FAST, statevector=True, program=prog).statevector
+    out["fast_vs_exact"] = _accuracy(fa, ex)
+    return out
+
+
+def qft(peak_gbs) -> List[Dict[str, object]]:
+    """QFT on 24 and 28 qubits: |x> (x uniform from the seed, prepared by X
+    gates), H + cp(pi/2^k) for every pair, the final SWAP network; 8192
+    shots; f64 and f32, exact and fast arithmetic. At 24 qubits the fast
+    state is compared with the exact one (bit-identical to the FP64 oracle)."""
+    rows = []
+    for n in (24, 28):
+        c, x = C.qft_circuit(n, 11)
+        p = c.to_program()
+        prog = zb.compile(p, 1)
+        for prec in (64, 32):
+            sv = {}
+            for mode, flags in (("exact", zb.FLAG_EXACT), ("fast", zb.FLAG_FAST)):
+                t, r = _timed_runs(p, prog, prec, flags, 8192, 3, 3)
+                d = device_profile(n, prec, flags, prog, 8192, 3, peak_gbs)
+                row = {"workload": "qft", "qubits": n, "precision": prec, "mode": mode, "seconds": t,
+                       "sweeps": r.sweeps, "launches": r.launches, "ops": len(prog.ops),
+                       "input_gates": prog.stats["input_gates"],
+                       "amp_updates_per_s": prog.stats["input_gates"] * 2.0 ** n / t, **d}
+                if n == 24:
+                    sv[mode] = zb.run(p, shots=0, precision=prec, flags=flags, statevector=True,
+                                      program=prog).statevector
+                rows.append(row)
+            if n == 24:
+                rows[-1]["fast_vs_exact"] = _accuracy(sv["fast"], sv["exact"])
+    return rows
+
+
+def fusion_sweep(peak_gbs, qubits=30, widths=(1, 2, 3, 4, 5)) -> List[Dict[str, object]]:
+    """30 qubits, depth 40, u3 + matching CX, f64 fast, 1024 shots, at fusion
+    widths K: one complete zc_run each; sweep GB/s = algorithmic bytes of
+    every state pass / wall seconds."""
+    p = C.matching_circuit(qubits, 40, 7).to_program()
+    rows = []
+    for k in widths:
+        prog = zb.compile(p, k)
+        t0 = time.perf_counter()
+        r = zb.run(p, shots=1024, seed=7, precision=64, flags=zb.FLAG_FAST, program=prog)
+        t = time.perf_counter() - t0
+        gbs = r.bytes_moved / t / 1e9
+        rows.append({"workload": "%dq depth-40 u3+matching-CX f64 fast" % qubits, "fusion": k, "seconds": t,
+                     "sim_seconds": r.sim_time, "ops": len(prog.ops), "max_fused": prog.stats["max_fused"],
+                     "sweeps": r.sweeps, "launches": r.launches, "pass_GBps": gbs,
+                     "roofline_frac": gbs / peak_gbs})
+    return rows
+
+
+def big_state(peak_gbs, qubits=33) -> Dict[str, object]:
+    """33 qubits (128 GiB f64 state), depth 40, f64 fast, fusion 1, 1024 shots."""
+    p = C.matching_circuit(qubits, 40, 7).to_program()
+    prog = zb.compile(p, 1)
+    t0 = time.perf_counter()
+    r = zb.run(p, shots=1024, seed=7, precision=64, flags=zb.FLAG_FAST, program=prog)
+    t = time.perf_counter() - t0
+    gbs = r.bytes_moved / t / 1e9
+    return {"workload": "%dq depth-40 u3+matching-CX f64 fast" % qubits, "state_GiB": 2.0 ** qubits * 16 / 2**30,
+            "seconds": t, "sim_seconds": r.sim_time, "sweeps": r.sweeps, "launches": r.launches,
+            "pass_GBps": gbs, "roofline_frac": gbs / peak_gbs}
+
+
+TRAJ_NOISE = dict(depolarizing_1q=1e-3, depolarizing_2q=1e-2, amplitude_damping=1e-3, readout_flip_0to1=0.02,
+                  readout_flip_1to0=0.02)
+
+
+def trajectories(peak_gbs) -> Dict[str, object]:
+    """16 qubits, depth 20 (u3 + matching CX), depolarizing 1e-3 after each
+    one-qubit gate and 1e-2 after each CX, amplitude damping 1e-3 on every
+    qubit a gate touches, after the gate (zeno's schedule,
+    src/noise.rs:163-174), symmetric 2% readout; 4096 trajectories as
+    batched f32 states in one launch, 1 shot each."""
+    noise = zb.NoiseModel(**TRAJ_NOISE)
+    p = C.matching_circuit(16, 20, 7).to_program()
+    prog = zb.compile(p, 0)
+    zb.run(p, shots=256, seed=1, precision=32, noise=noise, program=prog)
+    ts = []
+    for i in range(3):
+        t0 = time.perf_counter()
+        r = zb.run(p, shots=4096, seed=2 + i, precision=32, noise=noise, program=prog)
+        ts.append(time.perf_counter() - t0)
+    t = statistics.median(ts)
+    S = 2.0 ** 16 * 8
+    passes = len(prog.ops)
+    return {"workload": "16q depth-20 u3+matching-CX f32, dep 1e-3/1e-2, damping 1e-3 per touched qubit "
+                        "per gate, readout 2%, 4096 trajectories", "seconds": t, "trajectories_per_s": 4096 / t,
+            "launches": r.launches, "batched": r.batched, "ops": passes, "keys": len(r.counts),
+            "state_pass_GBps": 4096 * passes * 2 * S / t / 1e9,
+            "note": "state passes of every trajectory (2S per op, S = 512 KiB) over wall time; each "
+                    "trajectory's state stays in its CTA's L2-resident buffer, so this is not HBM traffic"}
+
+
+def gate_mix_tc(peak_gbs, tf32_tflops=None, qubits=28) -> Dict[str, object]:
+    """28 qubits, depth 60, gates per slot from {H, S, T, RX/RY/RZ, CX, CZ,
+    SWAP} with probabilities {.15, .1, .1, .3, .25, .05, .05}: unfused f32
+    sweeps and k = 5, 6, 7 blocks as 3xTF32 tensor-core GEMMs, each against
+    the f64 run (fast f64: within 1e-12 of exact, far below the f32 errors
+    measured here). Device times from the in-library profiler."""
+    n = qubits
+    p = C.mixed_circuit(n, 60, 7).to_program()
+    prog1 = zb.compile(p, 1)
+    ref = zb.run(p, shots=0, seed=1, precision=64, flags=zb.FLAG_FAST, statevector=True, program=prog1).statevector
+    S = 2.0 ** n * 8
+    out = {"workload": "%dq depth-60 gate mix" % n, "rows": []}
+    variants = [("f32 sweeps (fusion 1, FMA)", prog1, zb.FLAG_FAST, None)]
+    for k in (5, 6, 7):
+        variants.append(("f32 k=%d blocks on tcgen05 (3xTF32, FP32 accumulation)" % k, zb.compile(p, k),
+                         zb.FLAG_FAST | zb.FLAG_TENSOR, k))
+    for name, prog, flags, k in variants:
+        sv = zb.run(p, shots=0, seed=1, precision=32, flags=flags, statevector=True, program=prog).statevector
+        acc = _accuracy(sv, ref)
+        del sv
+        d = device_profile(n, 32, flags, prog, 1, 1, peak_gbs)
+        row = {"variant": name, "ops": len(prog.ops), "device_ms": d["device_ms"], "kernels": d["kernels"],
+               **{k2 + "_vs_f64": v for k2, v in acc.items()}}
+        if k is not None:
+            blocks = [op for op in prog.ops if op.kind == zb.OP_UNITARY and len(op.qubits) >= 4]
+            flops = sum(8.0 * 2.0 ** (n + len(op.qubits)) for op in blocks)
+            tc = d["kernels"].get("tc_block", {"launches": 0, "ms": 0.0})
+            row["tc_blocks"] = tc["launches"]
+            row["tc_ms_per_block"] = tc["ms"] / max(1, tc["launches"])
+            if tc["ms"]:
+                ach = flops / (tc["ms"] * 1e-3) / 1e12
+                ai = 2.0 ** (k - 1)  # flop per byte of a k-qubit block over 2S at f32
+                bound = min(peak_gbs * 1e9 * ai / 1e12, tf32_tflops / 3.0) if tf32_tflops else peak_gbs * 1e9 * ai / 1e12
+                row["tc_roofline"] = {"achieved_TFLOPs": ach, "bound_TFLOPs": bound, "frac": ach / bound,
+                                      "bound": "min(HBM x %g flop/B, TF32 peak / 3)" % ai if tf32_tflops
+                                      else "HBM x %g flop/B (TF32 peak not given)" % ai,
+                                      "block_GBps": 2 * S * tc["launches"] / (tc["ms"] * 1e-3) / 1e9}
+        out["rows"].append(row)
+    return out
+
+
+def serving(peak_gbs, requests=10000, rates=(10000.0, 1000.0, 100.0), low_rate_requests=1000,
+            tvd_samples=24) -> Dict[str, object]:
+    """The serving stream: Poisson arrivals, qubits log-uniform over 8..26,
+    gate-mix circuits of depth U[4, 60], shots log-uniform over 1..8192, 5%
+    of requests flagged for f64, seeds from a master seed. Each rate runs
+    the continuous-batching server and, in arrival order, one circuit per
+    call; rates whose stream would outlast the others (below 1000 req/s)
+    replay the first `low_rate_requests` requests. Programs are compiled
+    once and shared by every run (only arrival times depend on the rate).
+    Accuracy: f32 requests (up to 22 qubits) run alone at f32 and f64; the
+    output distributions' TVD and max |d amp|."""
+    from . import serve
+
+    base = serve.request_stream(requests, rate=rates[0], master_seed=2024)
+    t0 = time.perf_counter()
+    serve.compile_requests(base)
+    compile_s = time.perf_counter() - t0
+    out = {"workload": "%d requests, 8..26 qubits log-uniform, gate mix depth U[4,60], shots 1..8192, 5%% f64"
+                       % requests, "host_compile_s": compile_s, "rates": []}
+    for rate in rates:
+        count = requests if rate >= 1000.0 else min(requests, low_rate_requests)
+        srv_reqs = serve.request_stream(count, rate=rate, master_seed=2024)
+        pl_reqs = serve.request_stream(count, rate=rate, master_seed=2024)
+        for a, b, c in zip(srv_reqs, pl_reqs, base):
+            a.program = b.program = c.program
+        s = serve.serve_stream(srv_reqs)
+        pl = serve.plain_stream(pl_reqs)
+        out["rates"].append({"rate_per_s": rate, "requests": count, "server": s, "one_per_call": pl,
+                             "throughput_ratio": s["circuits_per_s"] / pl["circuits_per_s"],
+                             "p99_ratio": pl["p99_ms"] / s["p99_ms"] if s["p99_ms"] else None})
+    acc = []
+    for q in base:
+        if len(acc) >= tvd_samples:
+            break
+        if q.precision != 32 or q.n > 22:
+            continue
+        shell = C.Program(q.n, list(q.program.cregs), [])
+        a32 = zb.run(shell, shots=0, precision=32, flags=zb.FLAG_FAST, statevector=True, program=q.program)
+        a64 = zb.run(shell, shots=0, precision=64, flags=zb.FLAG_FAST, statevector=True, program=q.program)
+        acc.append({"qubits": q.n, "depth": q.depth, **_accuracy(a32.statevector, a64.statevector)})
+    out["f32_vs_f64"] = {"requests": len(acc), "max_tvd": max(a["tvd"] for a in acc) if acc else None,
+                         "max_abs_damp": max(a["max_abs_damp"] for a in acc) if acc else None,
+                         "per_request": acc}
+    return out

@@ -80,14 +80,17 @@ int zc_finish(zc_state *st);
 /* Backend::sample without any allocation (no counterpart in the reference).
  * For callers that cannot let the library allocate device memory when they
  * sample: runtimes that carve all device memory into their own pool at
- * start-up, loops that must not stall on cudaMalloc/cudaFree, or code that
- * is recording a stream capture. Same indices as zc_sample. Its scratch is
- * a fixed ~0.9 MiB device array that every GPU loading the library keeps
- * until exit. Limits: <= 30 qubits, <= 16384 shots; larger requests get
- * ZC_ERR_INVALID. Queued ops must be flushed first (zc_finish). The first
- * call on a device resolves the array's device address, so make that call
- * before any stream capture. All calls share the array: calls that overlap
- * (on the GPU or from several threads) race. */
+ * start-up, or loops that must not stall on cudaMalloc/cudaFree. It draws
+ * zeno's own indices — those of zc_sample on an exact-mode state — whatever
+ * arithmetic flag the state was created with (on a ZC_FLAG_FAST state,
+ * zc_sample's faster sums may move a draw by one index; this call does
+ * not). Its scratch is a fixed ~0.9 MiB device array that every GPU loading
+ * the library keeps until exit. Limits: <= 30 qubits, <= 16384 shots;
+ * larger requests get ZC_ERR_INVALID. Queued ops must be flushed first
+ * (zc_finish). The call synchronises the state's stream, so it must not be
+ * made on a stream that is being captured. The first call on a device
+ * resolves the array's device address. All calls share the array: calls
+ * that overlap (on the GPU or from several threads) race. */
 int zc_sample_noalloc(zc_state *st, uint64_t shots, uint64_t seed, uint64_t *out);
 
 /* Thread-local text of the last error. */
@@ -241,7 +244,8 @@ typedef struct {
 } zc_noise;
 
 typedef struct {
-    int precision_bits;   /* 32, 64, or 0 = auto (f64 if it fits the budget) */
+    int precision_bits;   /* 32, 64, or 0 = auto: f64 if it fits the budget, else f32 with zeno's
+                             auto-precision notice (resolve_precision, src/exec.rs:261-304) */
     uint32_t flags;       /* ZC_FLAG_* for the backend */
     uint64_t shots;
     uint64_t seed;
@@ -259,6 +263,7 @@ typedef struct {
     uint64_t launches;
     uint64_t sweeps;
     uint64_t bytes_moved;
+    char notices[512];     /* RunResult::notices (src/exec.rs:129), one per line, NUL-terminated */
 } zc_run_result;
 
 /* Run a compiled program. Counts are returned as (clbit word, count)

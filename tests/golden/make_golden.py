@@ -8,7 +8,8 @@ together with the expected output its header comment states. The tests
 replay these lists through the oracle and the CUDA backend; nothing at test
 time reads the reference checkout.
 
-Usage: python tests/golden/make_golden.py [/path/to/zeno/checkout]
+Usage: python tests/golden/make_golden.py /path/to/zeno/checkout
+       (or set ZENO_REFERENCE to the checkout)
 """
 
 import json
@@ -138,9 +139,6 @@ def parse(src):
     return {"n_qubits": sum(s for _, s in qregs), "cregs": cregs, "instrs": instrs}
 
 
-DEFAULT_REF = "/root/reference"
-
-
 def build(ref):
     """The fixture contents for the examples in the checkout at `ref`."""
     out = {}
@@ -153,7 +151,9 @@ def build(ref):
 
 
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF
+    ref = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("ZENO_REFERENCE")
+    if not ref:
+        sys.exit("usage: make_golden.py /path/to/zeno/checkout (or set ZENO_REFERENCE)")
     out = build(ref)
     with open(os.path.join(HERE, "examples.json"), "w") as f:
         json.dump(out, f, indent=1, sort_keys=True)

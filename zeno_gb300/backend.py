@@ -11,7 +11,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
-from dataclasses import dataclass, fields
+from dataclasses import dataclass, field, fields
 from typing import Dict, List, Optional, Sequence, Tuple
 
 import numpy as np
@@ -107,7 +107,8 @@ class RunOptions(C.Structure):
 
 class RunResultC(C.Structure):
     _fields_ = [("precision_bits", C.c_int), ("batched", C.c_int), ("n_keys", C.c_uint64), ("sim_seconds", C.c_double),
-                ("launches", C.c_uint64), ("sweeps", C.c_uint64), ("bytes_moved", C.c_uint64)]
+                ("launches", C.c_uint64), ("sweeps", C.c_uint64), ("bytes_moved", C.c_uint64),
+                ("notices", C.c_char * 512)]
 
 
 @dataclass
@@ -425,6 +426,7 @@ class RunResult:
     sweeps: int
     bytes_moved: int
     batched: bool = False
+    notices: List[str] = field(default_factory=list)
 
 
 def run(p, shots: int = 1024, seed: int = 0, precision: int = 0, fusion: Optional[int] = None,
@@ -458,7 +460,8 @@ def run(p, shots: int = 1024, seed: int = 0, precision: int = 0, fusion: Optiona
         fmt[key] = fmt.get(key, 0) + v
     prec = res.precision_bits
     return RunResult(fmt, raw, shots, p.n_qubits, prec, "cuda-f%d" % prec, seed, res.sim_seconds, sv,
-                     program.stats, res.launches, res.sweeps, res.bytes_moved, bool(res.batched))
+                     program.stats, res.launches, res.sweeps, res.bytes_moved, bool(res.batched),
+                     [x for x in res.notices.decode(errors="replace").split("\n") if x])
 
 
 def device_info() -> Dict[str, object]:

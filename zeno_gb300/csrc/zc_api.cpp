@@ -118,7 +118,6 @@ static int check_support(const zc_state *st, const uint32_t *qs, uint32_t k, uin
 
 static inline bool exact(const zc_state *st) { return (st->flags & ZC_FLAG_FAST) == 0; }
 
-static int check_device_error(zc_state *st);
 
 static int sync_read_scalar(zc_state *st, double *out) {
     ZC_CUDA(cudaMemcpyAsync(st->h_scalar, st->d_scalar, sizeof(double), cudaMemcpyDeviceToHost, st->stream));
@@ -496,7 +495,7 @@ static int enqueue(zc_state *st, QOp &&op) {
     return ZC_OK;
 }
 
-static int check_device_error(zc_state *st) {
+int check_device_error(zc_state *st) {
     int h[kErrWords] = {};
     ZC_CUDA(cudaMemcpyAsync(h, st->d_err, sizeof(h), cudaMemcpyDeviceToHost, st->stream));
     ZC_CUDA(cudaStreamSynchronize(st->stream));
@@ -651,17 +650,13 @@ int zc_device_info(zc_device *out) {
 
 int zc_create(uint32_t n, int prec, zc_state **out) { return zc_create_ex(n, prec, ZC_FLAG_EXACT, out); }
 
-int zc_create_ex(uint32_t n, int prec, uint32_t flags, zc_state **out) {
-    if (!out) return fail(ZC_ERR_INVALID, "null output handle");
-    *out = nullptr;
-    if (prec != 32 && prec != 64) return fail(ZC_ERR_INVALID, "precision_bits must be 32 or 64");
-    if (n < 1 || n > 48) return fail(ZC_ERR_INVALID, "qubit count must be in 1..=48");
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return fail(ZC_ERR_UNSUPPORTED, std::string("no usable CUDA device: ") + cudaGetErrorString(e));
-    uint64_t budget = 0;
-    int rc = zc_device_budget(0.75, &budget);
-    if (rc) return rc;
+}  // extern "C"
+
+namespace zc {
+
+// mem::plan (src/mem.rs:114-131): refuse a state above the budget, with the
+// text of zeno's Error::Memory.
+int plan_state(uint32_t n, int prec, uint64_t budget) {
     const uint64_t need = zc_state_bytes(n, prec);
     if (need > budget) {
         char buf[256];
@@ -672,6 +667,32 @@ int zc_create_ex(uint32_t n, int prec, uint32_t flags, zc_state **out) {
                  zc_max_qubits(budget, prec));
         return fail(ZC_ERR_MEMORY, buf);
     }
+    return ZC_OK;
+}
+
+}  // namespace zc
+
+extern "C" int zc_create_ex(uint32_t n, int prec, uint32_t flags, zc_state **out) {
+    if (!out) return fail(ZC_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    if (prec != 32 && prec != 64) return fail(ZC_ERR_INVALID, "precision_bits must be 32 or 64");
+    if (n < 1 || n > 48) return fail(ZC_ERR_INVALID, "qubit count must be in 1..=48");
+    uint64_t budget = 0;
+    int rc = zc_device_budget(0.75, &budget);
+    if (rc) return rc;
+    return create_state(n, prec, flags, budget, out);
+}
+
+int zc::create_state(uint32_t n, int prec, uint32_t flags, uint64_t budget, zc_state **out) {
+    if (!out) return fail(ZC_ERR_INVALID, "null output handle");
+    *out = nullptr;
+    if (prec != 32 && prec != 64) return fail(ZC_ERR_INVALID, "precision_bits must be 32 or 64");
+    if (n < 1 || n > 48) return fail(ZC_ERR_INVALID, "qubit count must be in 1..=48");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail(ZC_ERR_UNSUPPORTED, std::string("no usable CUDA device: ") + cudaGetErrorString(e));
+    int rc = plan_state(n, prec, budget);
+    if (rc) return rc;
     zc_state *st = new zc_state();
     st->n = n;
     st->prec = prec;
@@ -716,6 +737,8 @@ int zc_create_ex(uint32_t n, int prec, uint32_t flags, zc_state **out) {
     *out = st;
     return ZC_OK;
 }
+
+extern "C" {
 
 void zc_destroy(zc_state *st) {
     if (!st) return;

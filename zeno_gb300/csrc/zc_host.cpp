@@ -864,13 +864,38 @@ int zc_run(const zc_program *p, const zc_run_options *opt, zc_run_result *res, u
     if ((noise || p->dynamic) && sv)
         return fail(ZC_ERR_INVALID, noise ? "a noise model is active: the noisy state has no single final state vector"
                                           : "circuit is dynamic: it has no single final state vector");
-    // resolve_precision (src/exec.rs:261-304) against the HBM budget
+    // resolve_precision (src/exec.rs:261-304) against the HBM budget: an
+    // explicit precision must fit; auto takes f64 if it fits, else f32 with
+    // zeno's notice (and refuses if f32 does not fit either)
     uint64_t budget = 0;
     int rc = zc_device_budget(opt->mem_fraction > 0 ? opt->mem_fraction : 0.75, &budget);
     if (rc) return rc;
     int prec = opt->precision_bits;
-    if (prec == 0) prec = zc_state_bytes(p->n_qubits, 64) <= budget ? 64 : 32;
+    std::string notices;
+    auto notice = [&](const std::string &s) { notices += s + "\n"; };
+    if (prec != 0 && prec != 32 && prec != 64) return fail(ZC_ERR_INVALID, "precision_bits must be 0, 32 or 64");
+    if (prec == 0) {
+        if (zc_state_bytes(p->n_qubits, 64) <= budget) {
+            prec = 64;
+        } else {
+            prec = 32;
+            notice("auto-precision: " + std::to_string(p->n_qubits) +
+                   " qubits exceed the f64 budget, using f32 (8 B/amplitude)");
+        }
+    }
+    if ((rc = plan_state(p->n_qubits, prec, budget))) return rc;
     res->precision_bits = prec;
+    // run_inner / run_sampled / run_per_shot notices (src/exec.rs:374, :429-435, :478-481)
+    if (noise) notice("noise: trajectory sampling \xe2\x80\x94 per-shot execution, fusion disabled");
+    if (!p->dynamic && p->finals.empty() && opt->shots > 0)
+        notice(noise ? "circuit has no measurements: counts are empty"
+                     : "circuit has no measurements: counts are empty (use --statevector to inspect the state)");
+    auto put_notices = [&]() {
+        const size_t n = std::min(notices.size(), sizeof(res->notices) - 1);
+        memcpy(res->notices, notices.data(), n);
+        res->notices[n] = 0;
+    };
+    put_notices();
     const auto t0 = std::chrono::steady_clock::now();
     if ((noise || p->dynamic) && prec == 32 && !(opt->flags & ZC_FLAG_PER_SHOT) && batchable(p)) {
         std::vector<std::pair<uint64_t, uint64_t>> hist;
@@ -885,7 +910,7 @@ int zc_run(const zc_program *p, const zc_run_options *opt, zc_run_result *res, u
         return rc;
     }
     zc_state *st = nullptr;
-    rc = zc_create_ex(p->n_qubits, prec, opt->flags, &st);
+    rc = create_state(p->n_qubits, prec, opt->flags, budget, &st);
     if (rc) return rc;
     if (opt->sweep_high && (rc = zc_set_sweep_shape(st, opt->sweep_high))) {
         zc_destroy(st);

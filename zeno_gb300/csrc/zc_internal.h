@@ -106,6 +106,15 @@ struct ProfScope {
     ~ProfScope();
 };
 
+// Reads the state's device error record after a sync (a kernel that gave
+// up on a bounded wait or found an index out of range): ZC_ERR_CUDA with
+// the record's text, and the record cleared; else ZC_OK.
+int check_device_error(zc_state *st);
+// mem::plan against `budget` bytes (ZC_ERR_MEMORY with zeno's text), and
+// zc_create_ex with that budget in place of 0.75 of the device memory.
+int plan_state(uint32_t n, int prec, uint64_t budget);
+int create_state(uint32_t n, int prec, uint32_t flags, uint64_t budget, zc_state **out);
+
 int launch_1q(zc_state *st, uint32_t q, const double *m8, bool exact);
 int launch_kq(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat, bool exact);
 // Dense k-qubit block (k = 3..7) on tensor cores, f32 state, 3xTF32 (zc_tc.cu);

@@ -4,13 +4,17 @@
 // buffers that it grows with cudaMalloc on first use and whenever a larger
 // state or shot count arrives. Some callers cannot let a library allocate at
 // that point: an embedding runtime that carves all device memory into its
-// own pool at start-up and forbids later cudaMalloc, a serving loop that
+// own pool at start-up and forbids later cudaMalloc, or a serving loop that
 // must not stall on cudaMalloc / cudaFree (cudaFree synchronises the
-// device), or code that is recording a CUDA stream capture, during which
-// cudaMalloc is not permitted. zc_sample_noalloc draws exactly the same
-// indices as zc_sample, but all of its device scratch lives in one
+// device). zc_sample_noalloc draws the indices zeno's own sampler draws —
+// those of zc_sample on an exact-mode state, whatever arithmetic flag this
+// state was created with — but all of its device scratch lives in one
 // file-scope __device__ array of fixed size (kScratchBytes, about 0.9 MiB),
 // which every GPU that loads the library holds until the process exits.
+//
+// The call synchronises the state's stream (it routes the draws on the
+// host between its two kernels), so it must not be made on a stream that
+// is being captured into a CUDA graph.
 //
 // Limits: states of at most 30 qubits (16384 chunks of 2^16 amplitudes) and
 // at most 16384 shots per call; larger requests are refused.
@@ -86,30 +90,60 @@ __global__ void __launch_bounds__(64) k_masses_fixed(const T *__restrict__ re, c
     if (my_c < nchunks) part[my_c] = acc;
 }
 
-// Per touched chunk, the serial rescan of src/sample.rs:64-108.
+// Per touched chunk, the serial rescan of src/sample.rs:64-108, one warp per
+// chunk: the lanes load 32 consecutive amplitudes (coalesced) and square
+// them; lane 0 adds the squares into the running f64 sum in index order and
+// emits every draw below it, exactly as the serial loop does.
+constexpr int kScanThreads = 128;
+
 template <typename T>
-__global__ void k_scan_fixed(const T *__restrict__ re, const T *__restrict__ im, const SampleChunk *__restrict__ cs,
-                             uint64_t ncs, const double *__restrict__ us, uint64_t *__restrict__ out,
-                             uint64_t chunk_len, uint64_t total) {
-    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (t >= ncs) return;
-    const SampleChunk sc = cs[t];
+__global__ void __launch_bounds__(kScanThreads) k_scan_fixed(const T *__restrict__ re, const T *__restrict__ im,
+                                                             const SampleChunk *__restrict__ cs, uint64_t ncs,
+                                                             const double *__restrict__ us,
+                                                             uint64_t *__restrict__ out, uint64_t chunk_len,
+                                                             uint64_t total) {
+    const uint64_t w = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;  // warp-uniform
+    const int lane = threadIdx.x % 32;
+    if (w >= ncs) return;
+    const SampleChunk sc = cs[w];
     const uint64_t lo = sc.chunk * chunk_len, hi = lo + chunk_len < total ? lo + chunk_len : total;
-    uint64_t ptr = sc.s0;
+    uint64_t ptr = sc.s0;  // lane 0's cursor
     double acc = sc.cum;
-    for (uint64_t i = lo; i < hi; i++) {
-        acc = radd(acc, p2((double)re[i], (double)im[i]));
-        while (ptr < sc.s1 && us[ptr] < acc) out[ptr++] = i;
-        if (ptr == sc.s1) break;
+    double u = ptr < sc.s1 ? us[ptr] : 0.0;
+    int done = ptr >= sc.s1;
+    for (uint64_t base = lo; base < hi && !done; base += 32) {
+        const uint64_t i = base + lane;
+        const double v = i < hi ? p2((double)re[i], (double)im[i]) : 0.0;
+        for (int e = 0; e < 32; e++) {
+            const double x = __shfl_sync(0xffffffffu, v, e);
+            if (lane == 0 && !done && base + e < hi) {
+                acc = radd(acc, x);
+                while (u < acc) {
+                    out[ptr++] = base + e;
+                    if (ptr == sc.s1) {
+                        done = 1;
+                        break;
+                    }
+                    u = us[ptr];
+                }
+            }
+        }
+        done = __shfl_sync(0xffffffffu, done, 0);
     }
-    if (ptr < sc.s1) {
+    const uint64_t left = __shfl_sync(0xffffffffu, ptr, 0);
+    if (left < sc.s1) {  // leftover draws go to the chunk's last nonzero index
         uint64_t last_nz = hi - 1;
-        for (uint64_t i = hi; i-- > lo;)
-            if (p2((double)re[i], (double)im[i]) > 0.0) {
-                last_nz = i;
+        for (uint64_t top = hi; top > lo; top = top > lo + 32 ? top - 32 : lo) {
+            const bool in = top >= lo + 1 + (uint64_t)lane;
+            const uint64_t i = in ? top - 1 - lane : lo;
+            const unsigned m = __ballot_sync(0xffffffffu, in && p2((double)re[i], (double)im[i]) > 0.0);
+            if (m) {  // the lowest set lane holds the highest index
+                last_nz = top - 1 - (uint64_t)(__ffs(m) - 1);
                 break;
             }
-        while (ptr < sc.s1) out[ptr++] = last_nz;
+        }
+        if (lane == 0)
+            for (uint64_t k = left; k < sc.s1; k++) out[k] = last_nz;
     }
 }
 
@@ -161,13 +195,14 @@ int sample_fixed(zc_state *st, uint64_t shots, uint64_t seed, uint64_t *out, uns
     ZC_CUDA(cudaMemsetAsync(d_out, 0, shots * sizeof(uint64_t), st->stream));  // unresolved draws read 0
     if (ntouched) {
         ZC_CUDA(cudaMemcpyAsync(d_cs, h_chunks, ntouched * sizeof(SampleChunk), cudaMemcpyHostToDevice, st->stream));
-        k_scan_fixed<T><<<(int)((ntouched + 127) / 128), 128, 0, st->stream>>>(re, im, d_cs, ntouched, d_us, d_out,
-                                                                               chunk, st->len);
+        const uint64_t warps_per_cta = kScanThreads / 32;
+        k_scan_fixed<T><<<(int)((ntouched + warps_per_cta - 1) / warps_per_cta), kScanThreads, 0, st->stream>>>(
+            re, im, d_cs, ntouched, d_us, d_out, chunk, st->len);
         ZC_CUDA(cudaGetLastError());
     }
     ZC_CUDA(cudaMemcpyAsync(out, d_out, shots * sizeof(uint64_t), cudaMemcpyDeviceToHost, st->stream));
     ZC_CUDA(cudaStreamSynchronize(st->stream));
-    return ZC_OK;
+    return check_device_error(st);  // as zc_sample: a kernel that gave up left a wrong state
 }
 
 }  // namespace

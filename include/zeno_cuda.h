@@ -31,7 +31,9 @@ extern "C" {
 
 /* zc_create_ex flags */
 #define ZC_FLAG_EXACT 0u      /* reference arithmetic, no FMA: bit-exact with zeno's CPU kernels */
-#define ZC_FLAG_FAST 1u       /* FMA-contracted arithmetic (tolerance parity, not bit-exact) */
+#define ZC_FLAG_FAST 1u       /* tolerance parity, not bit-exact: f32 FMA-contracted (max |d amp| <= 1e-5
+                                 vs the f64 oracle); f64 in double-float pairs on the FP32 pipe with f64
+                                 storage (max |d amp| <= 1e-12) */
 #define ZC_FLAG_NO_SWEEPS 2u  /* one launch per op: disables multi-op sweep scheduling */
 #define ZC_FLAG_FORCE_SWEEPS 4u /* schedule sweeps even for small states (testing) */
 #define ZC_FLAG_PER_SHOT 8u   /* noisy runs: replay shot by shot (zeno's order and RNG) instead of batching */

@@ -200,3 +200,36 @@ def test_autotuned_runs_stay_bit_exact(zc, oracle):
     t = at.tune(p, 64, zc.FLAG_FAST, fusions=(1, 2), highs=(0, 5))
     assert min(r["seconds"] for r in t["table"]) == [r["seconds"] for r in t["table"]
                                                       if (r["fusion"], r["max_high"]) == (t["fusion"], t["max_high"])][0]
+
+
+@pytest.mark.parametrize("n", (9, 16))
+def test_fast_mode_f64_dense_blocks_within_1e12(zc, oracle, n):
+    """Fast f64 dense k-qubit blocks (k = 2..7, supports spanning low and
+    high qubits) run in double-float on the FP32 pipe: within 1e-12 of the
+    FP64 oracle, on random unitaries and a random normalised state."""
+    rng = np.random.default_rng(100 + n)
+    amps = rand_state(n, 13, normalize=True)
+    ops = []
+    for i in range(24):
+        k = 2 + i % 6
+        qs = sorted(int(x) for x in rng.choice(n, k, replace=False))
+        ops.append(("u", qs, np.linalg.qr(rand_matrix(1 << k, 900 + i))[0]))
+        if i % 3 == 0:
+            a, b = (int(x) for x in rng.choice(n, 2, replace=False))
+            ops.append(("cx", a, b))
+    g, o = replay(zc, oracle, n, 64, ops, zc.FLAG_FAST, amps)
+    d = np.abs(g.statevector() - o.statevector()).max()
+    assert d < 1e-12, d
+    g.close()
+
+
+@pytest.mark.parametrize("fusion", (2, 3, 5))
+def test_fast_mode_fused_circuit_vs_fp64_oracle(zc, oracle, fusion):
+    """The fused matching circuit at fusion width K in fast f64 (dense blocks
+    in double-float) against the oracle's FP64 run at the same K."""
+    p = C.matching_circuit(18, 10, 3).to_program()
+    _, _, sv, _ = oracle.run(p, prec=64, shots=0, fusion=fusion, statevector=True)
+    r = zc.run(p, shots=0, precision=64, fusion=fusion, statevector=True, flags=zc.FLAG_FAST)
+    d = np.abs(r.statevector - sv).max()
+    tvd = 0.5 * np.abs(np.abs(r.statevector) ** 2 - np.abs(sv) ** 2).sum()
+    assert d < 1e-12 and tvd < 1e-6, (fusion, d, tvd)

@@ -142,3 +142,45 @@ def test_per_shot_flag_reproduces_oracle_stream(zc, oracle):
     assert not r.batched
     ref = oracle.run(c.to_program(), prec=32, shots=300, seed=5, noise=noise)[0]
     assert r.counts == ref
+
+
+def _bits(counts, n):
+    """Shots as an (N, n) 0/1 array; bit j = clbit j (keys print clbit n-1 first)."""
+    rows = []
+    for k, v in counts.items():
+        b = [(int(k, 2) >> j) & 1 for j in range(n)]
+        rows.extend([b] * v)
+    return np.array(rows, dtype=np.int8)
+
+
+def test_config_shape_matches_per_shot_oracle(zc, oracle):
+    """The trajectory workload at its own shape — 16 qubits, depth 20 (u3 +
+    matching CX), depolarizing 1e-3 / 1e-2, amplitude damping 1e-3 per
+    touched qubit after each gate, 2% readout — against the oracle's
+    per-shot replay (zeno's run_per_shot). 2^16 outcomes are far more than
+    any affordable shot count resolves, so the comparison is on what the
+    shots do resolve: every qubit's P(1) at 6 sigma, and the 16-outcome
+    distribution of each block of four qubits by TVD within 6 sigma of the
+    TVD that sampling alone gives (the reference's own noisy-parity check
+    compares 16-outcome distributions by TVD, tests/noise.rs:703-735)."""
+    noise = zc.NoiseModel(depolarizing_1q=1e-3, depolarizing_2q=1e-2, amplitude_damping=1e-3,
+                          readout_flip_0to1=0.02, readout_flip_1to0=0.02)
+    n = 16
+    p = C.matching_circuit(n, 20, 7).to_program()
+    ng, no = 1 << 17, 2048
+    g = _bits(batched(zc, p, ng, 21, noise).counts, n)
+    o = _bits(oracle.run(p, prec=32, shots=no, seed=22, noise=noise)[0], n)
+    assert g.shape == (ng, n) and o.shape == (no, n)
+    pg, po = g.mean(axis=0), o.mean(axis=0)
+    for q in range(n):
+        sig = math.sqrt(max(pg[q] * (1 - pg[q]), 1e-12) * (1.0 / ng + 1.0 / no))
+        assert abs(pg[q] - po[q]) <= 6 * sig, (q, pg[q], po[q], sig)
+    w = 1 << np.arange(4)
+    for b0 in range(0, n, 4):
+        hg = np.bincount(g[:, b0:b0 + 4] @ w, minlength=16) / ng
+        ho = np.bincount(o[:, b0:b0 + 4] @ w, minlength=16) / no
+        d = 0.5 * np.abs(hg - ho).sum()
+        var = hg * (1 - hg) * (1.0 / ng + 1.0 / no)  # variance of each outcome's difference
+        mean = 0.5 * np.sum(np.sqrt(2 / np.pi * var))  # E|N(0, var)| = sqrt(2 var / pi)
+        std = 0.5 * np.sqrt(np.sum((1 - 2 / np.pi) * var))
+        assert d <= mean + 6 * std, (b0, d, mean, std)

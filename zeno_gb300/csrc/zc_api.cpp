@@ -151,6 +151,21 @@ int launch_single(zc_state *st, const QOp &op) {
             if (op.k >= 3 && st->prec == 32 && (st->flags & ZC_FLAG_TENSOR))
                 return launch_block_tc(st, op.qs, op.k, op.data.data());
             const void *dev = nullptr;
+            if (st->prec == 64 && !ex) {  // fast f64: double-float on the FP32 pipe
+                const size_t cnt = (size_t)1 << (2 * op.k);
+                std::vector<float> t(4 * cnt);
+                for (size_t i = 0; i < cnt; i++) {
+                    for (int part = 0; part < 2; part++) {  // re, im: hi = nearest float, lo = the rest
+                        const double x = op.data[2 * i + part];
+                        const float hi = (float)x;
+                        t[4 * i + 2 * part] = hi;
+                        t[4 * i + 2 * part + 1] = (float)(x - (double)hi);
+                    }
+                }
+                int rc = arena_put(st, t.data(), t.size() * sizeof(float), &dev);
+                if (rc) return rc;
+                return launch_kq_df(st, op.qs, op.k, dev);
+            }
             int rc = stage_table(st, op.data.data(), (size_t)1 << (2 * op.k), &dev);
             if (rc) return rc;
             return launch_kq(st, op.qs, op.k, dev, ex);

@@ -204,6 +204,103 @@ int run_kq(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat) {
     return ZC_OK;
 }
 
+// Fused k-qubit unitary on an f64 state in fast mode: the same gather /
+// row sums / scatter as k_kq, in double-float arithmetic on the FP32 pipe
+// (GB300 issues FP64 ~68x slower than FP32). Amplitudes are split into
+// (hi, lo) pairs as they are staged; the matrix comes pre-split as float4
+// (re hi, re lo, im hi, im lo) per entry. Each output is a complex dot
+// product accumulated in unnormalised pairs, renormalised every 8 terms
+// and rounded back to f64 on the way out.
+constexpr int kKqDfTile = 1024;  // amplitudes staged per CTA iteration
+
+__global__ void __launch_bounds__(kThreads) k_kq_df(double *__restrict__ re, double *__restrict__ im, KqParams p,
+                                                    const float4 *__restrict__ mat) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int dim = 1 << p.k;
+    const int G = kKqDfTile / dim;
+    const int ld = dim + 1;  // padded row: conflict-free column walks
+    float2 *xr = reinterpret_cast<float2 *>(smem_raw);
+    float2 *xi = xr + G * ld;
+    double *yr = reinterpret_cast<double *>(xi + G * ld);
+    double *yi = yr + G * ld;
+    const uint64_t ntiles = (p.groups + G - 1) / G;
+    for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const uint64_t g0 = tile * G;
+        for (int e = threadIdx.x; e < G * dim; e += blockDim.x) {
+            const int gl = e % G, j = e / G;
+            const uint64_t g = g0 + gl;
+            if (g < p.groups) {
+                const uint64_t idx = insert_zeros(g, p.qs, p.k) | p.offs[j];
+                xr[gl * ld + j] = df_from_f64(re[idx]);
+                xi[gl * ld + j] = df_from_f64(im[idx]);
+            }
+        }
+        __syncthreads();
+        for (int o = threadIdx.x; o < G * dim; o += blockDim.x) {
+            const int gl = o % G, r = o / G;
+            if (g0 + gl < p.groups) {
+                float2 ar = make_float2(0.f, 0.f), ai = make_float2(0.f, 0.f);
+                const float4 *w = mat + (size_t)r * dim;
+                const float2 *x_r = xr + gl * ld, *x_i = xi + gl * ld;
+                for (int c = 0; c < dim; c++) {
+                    const float4 wc = __ldg(w + c);
+                    const float2 wr = make_float2(wc.x, wc.y), wi = make_float2(wc.z, wc.w);
+                    const float2 vr = x_r[c], vi = x_i[c];
+                    // (ar, ai) += (wr + i wi)(vr + i vi)
+                    ar = df_axpy_u(ar, wr, vr);
+                    ar = df_axpy_u(ar, df_neg(wi), vi);
+                    ai = df_axpy_u(ai, wr, vi);
+                    ai = df_axpy_u(ai, wi, vr);
+                    if ((c & 7) == 7) {
+                        ar = df_renorm(ar);
+                        ai = df_renorm(ai);
+                    }
+                }
+                yr[gl * ld + r] = df_to_f64(df_renorm(ar));
+                yi[gl * ld + r] = df_to_f64(df_renorm(ai));
+            }
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < G * dim; e += blockDim.x) {
+            const int gl = e % G, j = e / G;
+            const uint64_t g = g0 + gl;
+            if (g < p.groups) {
+                const uint64_t idx = insert_zeros(g, p.qs, p.k) | p.offs[j];
+                re[idx] = yr[gl * ld + j];
+                im[idx] = yi[gl * ld + j];
+            }
+        }
+        __syncthreads();
+    }
+}
+
+int run_kq_df(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat) {
+    KqParams p{};
+    p.k = k;
+    p.groups = st->len >> k;
+    for (uint32_t i = 0; i < k; i++) p.qs[i] = qs[i];
+    const int dim = 1 << k;
+    for (int j = 0; j < dim; j++) {
+        uint64_t o = 0;
+        for (uint32_t b = 0; b < k; b++)
+            if ((j >> b) & 1) o |= 1ull << qs[b];
+        p.offs[j] = o;
+    }
+    const int G = kKqDfTile / dim;
+    const size_t smem = (size_t)G * (dim + 1) * (2 * sizeof(float2) + 2 * sizeof(double));
+    static std::atomic<bool> attr_set{false};  // once per process
+    if (!attr_set) {
+        ZC_CUDA(cudaFuncSetAttribute(k_kq_df, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
+        attr_set = true;
+    }
+    const uint64_t ntiles = (p.groups + G - 1) / G;
+    const int blocks = (int)std::min<uint64_t>(ntiles, (uint64_t)st->num_sms * 3);
+    k_kq_df<<<blocks, kThreads, smem, st->stream>>>((double *)st->re, (double *)st->im, p,
+                                                    (const float4 *)dev_mat);
+    ZC_CUDA(cudaGetLastError());
+    return ZC_OK;
+}
+
 // ---------------------------------------------------------------- diagonals
 
 // 1-qubit diagonal (kern_diag1_scalar, src/state.rs:498-527).
@@ -420,6 +517,15 @@ int launch_kq(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat,
     if (st->prec == 64)
         return exact ? run_kq<double, true>(st, qs, k, dev_mat) : run_kq<double, false>(st, qs, k, dev_mat);
     return exact ? run_kq<float, true>(st, qs, k, dev_mat) : run_kq<float, false>(st, qs, k, dev_mat);
+}
+
+int launch_kq_df(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat_df) {
+    ProfScope ps(st, K_KQ, 2.0 * st->len * (st->prec / 8) * 2);
+    st->ctr.launches++;
+    st->ctr.sweeps++;
+    st->ctr.bytes_moved += 2 * st->len * (st->prec / 8) * 2;
+    if (st->prec != 64) return fail(ZC_ERR_INVALID, "double-float dense blocks need an f64 state");
+    return run_kq_df(st, qs, k, dev_mat_df);
 }
 
 int launch_diag1(zc_state *st, uint32_t q, const double *d4, bool exact) {

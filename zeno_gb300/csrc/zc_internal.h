@@ -117,6 +117,10 @@ int create_state(uint32_t n, int prec, uint32_t flags, uint64_t budget, zc_state
 
 int launch_1q(zc_state *st, uint32_t q, const double *m8, bool exact);
 int launch_kq(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat, bool exact);
+// Dense k-qubit block (k = 2..7) on an f64 state in fast mode, double-float
+// on the FP32 pipe; dev_mat_df: row-major 2^k x 2^k float4 (re hi, re lo,
+// im hi, im lo) per entry.
+int launch_kq_df(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat_df);
 // Dense k-qubit block (k = 3..7) on tensor cores, f32 state, 3xTF32 (zc_tc.cu);
 // mat: row-major 2^k x 2^k complex (interleaved f64 pairs).
 int launch_block_tc(zc_state *st, const uint32_t *qs, uint32_t k, const double *mat);

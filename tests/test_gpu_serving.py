@@ -1,8 +1,10 @@
 """Continuous-batching server: each result equals the result of running the
 same request alone (exact mode: identical counts; fast mode: the same draws
-on states that agree within tolerance, TVD <= 0.02), admission respects
-the HBM pool and slot limits, and arrivals during execution are admitted
-and overlap with requests already on the device."""
+on states that agree within the f32 tolerance, so at most 0.2% of the draws
+— and never more than a couple in small samples — land on a neighbouring
+outcome), admission respects the HBM pool and slot limits, and arrivals
+during execution are admitted and overlap with requests already on the
+device."""
 
 import numpy as np
 import pytest
@@ -51,11 +53,13 @@ def test_results_same_alone_and_in_the_mix(zc, flags):
             assert got[rid] == alone, (n, prec)  # program order kept: bit-identical states
         else:
             # fast mode may regroup commuting ops differently alone and in the mix; the
-            # states then agree within the fast-mode tolerance, so the same draws land
-            # on the same outcomes except within that tolerance of a boundary
+            # states then agree within the fast-mode tolerance (relative ~1e-7 per
+            # amplitude at f32), so a draw (same seed, same uniforms) moves only when it
+            # falls within that of a cumulative boundary: for n <= 20 the expected
+            # share is ~1e-4 of the draws. Each moved draw changes the TVD by 1/shots.
             keys = set(alone) | set(got[rid])
-            tvd = 0.5 * sum(abs(alone.get(k, 0) - got[rid].get(k, 0)) for k in keys) / shots
-            assert tvd <= 0.02, (n, prec, tvd)
+            moved = 0.5 * sum(abs(alone.get(k, 0) - got[rid].get(k, 0)) for k in keys)
+            assert moved <= max(2, 0.002 * shots), (n, prec, moved, shots)
     srv.close()
 
 

@@ -455,6 +455,17 @@ void consume_plan(std::vector<QOp> &q, SweepPlan &plan) {
     }
 }
 
+static bool sweepable(const QOp &op);
+static bool sweeps_enabled(const zc_state *st);
+
+// Before any kernel other than a sweep: a state that double-float sweeps
+// left as (hi, lo) pairs goes back to f64.
+static int settle_form(zc_state *st) {
+    if (!st->df_resident) return ZC_OK;
+    st->df_resident = false;
+    return launch_df_to_f64(st);
+}
+
 // Plan and launch one sweep starting at the queue front; erases what ran.
 static int run_one_sweep(zc_state *st) {
     std::vector<QOp> &q = st->queue;
@@ -462,7 +473,9 @@ static int run_one_sweep(zc_state *st) {
     SweepPlan plan;
     if (plan_sweep(st->n, st->prec, exact(st), sh.L, sh.Hcap, q, &plan) <= 1) {
         // nothing to batch: the per-op kernel is the same work
-        int rc = launch_single(st, q.front());
+        int rc = settle_form(st);
+        if (rc) return rc;
+        rc = launch_single(st, q.front());
         q.erase(q.begin());
         return rc;
     }
@@ -474,10 +487,17 @@ static int run_one_sweep(zc_state *st) {
     const void *dev = nullptr;
     int rc = arena_put(st, blob.data(), blob.size(), &dev);
     if (rc) return rc;
+    consume_plan(q, plan);
+    // Fast f64: consecutive sweeps of one flush hand the state over as
+    // (hi, lo) float pairs; the last one (nothing sweepable queued behind
+    // it) rounds it back to f64.
+    const bool df = st->prec == 64 && !exact(st);
+    const bool out_df = df && !q.empty() && sweepable(q.front());
+    plan.g.form = (st->df_resident ? kFormInDf : 0u) | (out_df ? kFormOutDf : 0u);
     rc = launch_sweep(st, plan.g, (const MicroOp *)dev, (int)plan.mops.size(), (const char *)dev + tab_off,
                       exact(st));
+    st->df_resident = out_df;
     for (const MicroOp &m : plan.mops) st->ctr.micro_ops[m.kind & 7]++;
-    consume_plan(q, plan);
     return rc;
 }
 
@@ -492,14 +512,16 @@ static int flush(zc_state *st) {
     int rc = ZC_OK;
     while (!st->queue.empty() && rc == ZC_OK) {
         if (!sweeps_enabled(st) || !sweepable(st->queue.front())) {
-            rc = launch_single(st, st->queue.front());
+            rc = settle_form(st);
+            if (rc == ZC_OK) rc = launch_single(st, st->queue.front());
             st->queue.erase(st->queue.begin());
             continue;
         }
         rc = run_one_sweep(st);
     }
     st->queue.clear();
-    return rc;
+    const int rc2 = settle_form(st);  // every other entry point sees f64
+    return rc ? rc : rc2;
 }
 
 static int enqueue(zc_state *st, QOp &&op) {

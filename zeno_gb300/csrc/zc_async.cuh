@@ -7,8 +7,8 @@
 namespace zc {
 namespace {
 
-constexpr unsigned kSpinLimit = 1u << 26;  // bounded mbarrier waits: polls
-constexpr uint64_t kWaitNs = 2000000000ull; // and wall time (2 s)
+constexpr unsigned kSpinLimit = 1u << 26;           // bounded mbarrier waits: polls
+constexpr long long kWaitCycles = 4000000000ll;      // and SM clock cycles (2 s at 2 GHz)
 
 __device__ __forceinline__ uint32_t smem_addr(const void *p) {
     return (uint32_t)__cvta_generic_to_shared(p);
@@ -23,17 +23,14 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                  : "memory");
 }
 
-__device__ __forceinline__ uint64_t global_ns() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
 // Bounded wait on phase `parity`: gives up after kSpinLimit polls or
-// kWaitNs of wall time, whichever comes first; returns false then.
+// kWaitCycles of the SM's cycle counter, whichever comes first; returns false
+// then. The SM counter only moves forward; %globaltimer follows the host's
+// clock and can step when the driver re-synchronises it, which could end a
+// wait early.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
     const uint32_t a = smem_addr(bar);
-    const uint64_t t0 = global_ns();
+    const long long t0 = clock64();
     for (unsigned it = 0; it < kSpinLimit; ++it) {
         uint32_t done;
         asm volatile(
@@ -44,7 +41,7 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
             : "r"(a), "r"(parity)
             : "memory");
         if (done) return true;
-        if ((it & 63) == 63 && global_ns() - t0 > kWaitNs) break;
+        if ((it & 63) == 63 && clock64() - t0 > kWaitCycles) break;
     }
     return false;
 }

@@ -86,6 +86,7 @@ struct zc_state {
     void *d_samp = nullptr;      // sampler work area
     size_t samp_cap = 0;
     int *d_err = nullptr;        // device error flag (sweep wait timeouts)
+    bool df_resident = false;    // inside a flush: fast f64 sweeps left (hi, lo) float pairs in re / im
     std::vector<zc::QOp> queue;  // ops waiting to be scheduled into sweeps
     bool prof = false;            // record CUDA events around every launch
     std::vector<zc::ProfRec> prof_recs;
@@ -179,6 +180,8 @@ void lower_df(const std::vector<const QOp *> &seq, int run_cap, std::vector<Lowe
 int launch_single(zc_state *st, const QOp &op);
 int launch_sweep_multi(cudaStream_t stream, int num_sms, int prec, bool exact, const char *dev_blob, int *d_err);
 int arena_put(zc_state *st, const void *src, size_t bytes, const void **dev);
+// Round an f64 state left as double-float pairs (g.form kFormOutDf) back to f64.
+int launch_df_to_f64(zc_state *st);
 int launch_sweep(zc_state *st, const SweepGeom &g, const MicroOp *dev_ops, int nops, const char *dev_tables,
                  bool exact);
 struct TrajOp;

@@ -585,7 +585,7 @@ __device__ __forceinline__ uint64_t row_offset(const SweepSmem<T, A> &c, uint32_
 // shared memory, TMA row stores. Returns false if a wait ran out.
 template <typename T, int A>
 __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const char *tables, T *sre, T *sim,
-                             uint32_t &phase) {
+                             uint32_t &phase, uint32_t form) {
     const uint32_t size = 1u << (c.L + c.H);
     const uint32_t rows = 1u << c.H, row_elems = 1u << c.L, row_bytes = row_elems * (uint32_t)sizeof(T);
     const int tid = threadIdx.x, warp = tid / 32, lane = tid % 32;
@@ -608,21 +608,41 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
     if (c.fail) return false;
     phase ^= 1;
     if constexpr (A == AR_DF) {
+        // The slots hold f64, or (form & kFormInDf) the normalised pairs the
+        // previous sweep left; on exit f64, or (form & kFormOutDf) normalised
+        // pairs. CX / SWAP move slots whatever they hold.
         double *dr = reinterpret_cast<double *>(sre), *di = reinterpret_cast<double *>(sim);
         float2 *fr = reinterpret_cast<float2 *>(sre), *fi = reinterpret_cast<float2 *>(sim);
-        if (c.has_arith && !c.fuse_in) {
+        const bool in_df = form & kFormInDf, out_df = form & kFormOutDf;
+        const bool fuse_in = c.fuse_in && !in_df, fuse_out = c.fuse_out && !out_df;
+        if (c.has_arith && !in_df && !c.fuse_in) {
             for (uint32_t v = tid; v < size; v += blockDim.x) {
                 fr[v] = df_from_f64(dr[v]);
                 fi[v] = df_from_f64(di[v]);
             }
             __syncthreads();
         }
-        apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut, c.gi, c.fuse_in,
-                                c.fuse_out);
-        if (c.has_arith && !c.fuse_out) {  // register passes leave pairs unnormalised
+        apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut, c.gi, fuse_in,
+                                fuse_out);
+        if (c.has_arith && !fuse_out) {  // register passes leave pairs unnormalised
             for (uint32_t v = tid; v < size; v += blockDim.x) {
-                dr[v] = df_to_f64(df_renorm(fr[v]));
-                di[v] = df_to_f64(df_renorm(fi[v]));
+                if (out_df) {
+                    fr[v] = df_renorm(fr[v]);
+                    fi[v] = df_renorm(fi[v]);
+                } else {
+                    dr[v] = df_to_f64(df_renorm(fr[v]));
+                    di[v] = df_to_f64(df_renorm(fi[v]));
+                }
+            }
+        } else if (!c.has_arith && in_df != out_df) {  // permutations only: change the form alone
+            for (uint32_t v = tid; v < size; v += blockDim.x) {
+                if (in_df) {
+                    dr[v] = df_to_f64(df_renorm(fr[v]));
+                    di[v] = df_to_f64(df_renorm(fi[v]));
+                } else {
+                    fr[v] = df_from_f64(dr[v]);
+                    fi[v] = df_from_f64(di[v]);
+                }
             }
         }
     } else {
@@ -684,7 +704,10 @@ __device__ void sweep_exit(SweepSmem<T, A> &c, uint32_t phase, int *err) {
 
 // One state. One CTA streams tiles through a single shared-memory buffer;
 // three CTAs per SM overlap one tile's TMA traffic with the others' arithmetic.
-template <typename T, int A>
+// FORM (g.form as a compile-time constant): each hand-over of double-float
+// pairs between sweeps is its own instantiation, so the tile loop carries no
+// run-time branches for it (they cost registers at the 80-register cap).
+template <typename T, int A, uint32_t FORM>
 __global__ void __launch_bounds__(kSweepThreads, kSweepCtasPerSm)
     k_sweep(T *__restrict__ re, T *__restrict__ im, const SweepGeom g, const MicroOp *__restrict__ gops, int nops,
             const char *__restrict__ tables, int *__restrict__ err) {
@@ -696,7 +719,7 @@ __global__ void __launch_bounds__(kSweepThreads, kSweepCtasPerSm)
     load_job(c, gops, nops, g.L, g.H, g.hpos, true);
     uint32_t phase = 0;
     for (uint64_t t = blockIdx.x; t < g.ntiles; t += gridDim.x)
-        if (!process_tile(c, re, im, t, tables, sre, sim, phase)) break;
+        if (!process_tile(c, re, im, t, tables, sre, sim, phase, FORM)) break;
     sweep_exit(c, phase, err);
 }
 
@@ -739,28 +762,42 @@ __global__ void __launch_bounds__(kSweepThreads, kSweepCtasPerSm)
         T *sre = reinterpret_cast<T *>(smem);
         T *sim = sre + (1u << (J.L + J.H));
         if (!process_tile(c, reinterpret_cast<T *>(J.re), reinterpret_cast<T *>(J.im), t - J.tile_start,
-                          blob + J.tables_off, sre, sim, phase))
+                          blob + J.tables_off, sre, sim, phase, 0u))
             break;
     }
     sweep_exit(c, phase, err);
 }
 
-template <typename T, int A>
-int run_sweep(zc_state *st, const SweepGeom &g, const MicroOp *dev_ops, int nops, const char *dev_tables) {
+template <typename T, int A, uint32_t FORM>
+int run_sweep_form(zc_state *st, const SweepGeom &g, const MicroOp *dev_ops, int nops, const char *dev_tables) {
     const size_t smem = (size_t)2 * (1u << (g.L + g.H)) * sizeof(T);
     static std::atomic<bool> attr{false};  // set once per process; racing first calls repeat it
     if (!attr) {
-        ZC_CUDA(cudaFuncSetAttribute(k_sweep<T, A>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        ZC_CUDA(cudaFuncSetAttribute(k_sweep<T, A, FORM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)kSweepSmemBytes));
         attr = true;
     }
     if (smem > kSweepSmemBytes || g.H > kMaxSweepHigh || nops > kMaxMicroOps)
         return fail(ZC_ERR_INVALID, "sweep shape exceeds the kernel's limits");
     const uint64_t blocks = std::min<uint64_t>(g.ntiles, (uint64_t)st->num_sms * kSweepCtasPerSm);
-    k_sweep<T, A><<<(int)blocks, kSweepThreads, smem, st->stream>>>((T *)st->re, (T *)st->im, g, dev_ops, nops,
-                                                                       dev_tables, st->d_err);
+    k_sweep<T, A, FORM><<<(int)blocks, kSweepThreads, smem, st->stream>>>((T *)st->re, (T *)st->im, g, dev_ops,
+                                                                             nops, dev_tables, st->d_err);
     ZC_CUDA(cudaGetLastError());
     return ZC_OK;
+}
+
+template <typename T, int A>
+int run_sweep(zc_state *st, const SweepGeom &g, const MicroOp *dev_ops, int nops, const char *dev_tables) {
+    if constexpr (A == AR_DF) {
+        switch (g.form) {
+            case 0: return run_sweep_form<T, A, 0>(st, g, dev_ops, nops, dev_tables);
+            case kFormInDf: return run_sweep_form<T, A, kFormInDf>(st, g, dev_ops, nops, dev_tables);
+            case kFormOutDf: return run_sweep_form<T, A, kFormOutDf>(st, g, dev_ops, nops, dev_tables);
+            default: return run_sweep_form<T, A, kFormInDf | kFormOutDf>(st, g, dev_ops, nops, dev_tables);
+        }
+    }
+    if (g.form) return fail(ZC_ERR_INVALID, "double-float hand-over requested outside a double-float sweep");
+    return run_sweep_form<T, A, 0>(st, g, dev_ops, nops, dev_tables);
 }
 
 template <typename T, int A>
@@ -776,7 +813,34 @@ int run_sweep_multi(cudaStream_t stream, int num_sms, const char *dev_blob, int 
     return ZC_OK;
 }
 
+// Round a state that double-float sweeps left as (hi, lo) pairs back to f64
+// (the last sweep of a flush normally does this itself; this pass serves a
+// flush whose double-float sweeps are followed by another kernel).
+__global__ void __launch_bounds__(256) k_df_to_f64(double *__restrict__ re, double *__restrict__ im, uint64_t len) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len; i += (uint64_t)gridDim.x * blockDim.x) {
+        const double2 a = reinterpret_cast<const double2 *>(re)[i];
+        const double2 b = reinterpret_cast<const double2 *>(im)[i];
+        const float4 fa = *reinterpret_cast<const float4 *>(&a), fb = *reinterpret_cast<const float4 *>(&b);
+        reinterpret_cast<double2 *>(re)[i] = make_double2(df_to_f64(df_renorm(make_float2(fa.x, fa.y))),
+                                                          df_to_f64(df_renorm(make_float2(fa.z, fa.w))));
+        reinterpret_cast<double2 *>(im)[i] = make_double2(df_to_f64(df_renorm(make_float2(fb.x, fb.y))),
+                                                          df_to_f64(df_renorm(make_float2(fb.z, fb.w))));
+    }
+}
+
 }  // namespace
+
+int launch_df_to_f64(zc_state *st) {
+    ProfScope ps(st, K_SWEEP, 2.0 * st->len * 8 * 2);
+    st->ctr.launches++;
+    st->ctr.sweeps++;
+    st->ctr.bytes_moved += 2 * st->len * 8 * 2;
+    const uint64_t n2 = st->len / 2;  // two elements per thread step; len >= 2^14 for sweeps
+    const uint64_t blocks = std::min<uint64_t>((n2 + 255) / 256, (uint64_t)st->num_sms * 8);
+    k_df_to_f64<<<(int)blocks, 256, 0, st->stream>>>((double *)st->re, (double *)st->im, n2);
+    ZC_CUDA(cudaGetLastError());
+    return ZC_OK;
+}
 
 int launch_sweep_multi(cudaStream_t stream, int num_sms, int prec, bool exact, const char *dev_blob, int *d_err) {
     if (prec == 64)

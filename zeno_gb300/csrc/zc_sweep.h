@@ -13,8 +13,12 @@ constexpr size_t kSweepSmemBytes = 64 * 1024;  // one tile buffer: 2^12 f64 or 2
 enum : uint32_t { MOP_U1 = 1, MOP_D1 = 2, MOP_DK = 3, MOP_CX = 4, MOP_SWAP = 5, MOP_R1 = 6, MOP_RT = 7 };
 
 // Tile geometry: local qubits are 0..L-1 plus hpos[0..H) (ascending).
+// form (double-float sweeps of f64 states): kFormInDf — the state holds
+// (hi, lo) float pairs on entry (the previous sweep left them); kFormOutDf —
+// leave normalised pairs for the next sweep instead of rounding to f64.
+constexpr uint32_t kFormInDf = 1u, kFormOutDf = 2u;
 struct SweepGeom {
-    uint32_t n, L, H, pad;
+    uint32_t n, L, H, form;
     uint32_t hpos[16];
     uint64_t ntiles;
 };

@@ -37,11 +37,12 @@ sys.path.insert(0, ROOT)
 
 METRIC = "30q circuit throughput (u3 + matching-CX, depth 40, f64)"
 # DRAM read+write per launch over algorithmic bytes, from an ncu capture of
-# the f64 double-float sweep kernel at 26 qubits (state 8x the L2):
-# 1.074 GB read + 1.027 GB write against 2S = 2.147 GB.
-MEASURED_TRAFFIC_RATIO = {"sweep": (1.074e9 + 1.027e9) / 2.147e9}
-# The same capture: issue slots 58% busy, FMA pipe 37%, ALU pipe 31%, FP64 0%.
-SWEEP_DF_PIPES = {"issue_active_pct": 57.6, "fma_pipe_pct": 36.5, "alu_pipe_pct": 30.9, "fp64_pipe_pct": 0.0}
+# the f64 double-float sweep kernel at 26 qubits (state 8x the L2; the sweeps
+# between the first and the last of a flush, which hand the state over as
+# double-float pairs): 1.074 GB read + 1.025 GB write against 2S = 2.147 GB.
+MEASURED_TRAFFIC_RATIO = {"sweep": (1.074e9 + 1.025e9) / 2.147e9}
+# The same capture: issue slots 58-61% busy, FMA pipe 41-42%, ALU pipe 22-23%, FP64 0%.
+SWEEP_DF_PIPES = {"issue_active_pct": 58.2, "fma_pipe_pct": 40.9, "alu_pipe_pct": 21.9, "fp64_pipe_pct": 0.0}
 # FP32 instructions per amplitude of each double-float sweep micro-op
 # (zeno_gb300/csrc/zc_arith.cuh): a product is 4 (FMUL + 3 FFMA), TwoSum 6,
 # renormalisation 3. Complex 2x2: four 4-term dot products per pair

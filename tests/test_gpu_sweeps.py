@@ -233,3 +233,34 @@ def test_fast_mode_fused_circuit_vs_fp64_oracle(zc, oracle, fusion):
     d = np.abs(r.statevector - sv).max()
     tvd = 0.5 * np.abs(np.abs(r.statevector) ** 2 - np.abs(sv) ** 2).sum()
     assert d < 1e-12 and tvd < 1e-6, (fusion, d, tvd)
+
+
+@pytest.mark.parametrize("prec,tol", ((64, 1e-12), (32, 1e-5)))
+def test_fast_mode_deep_circuit_vs_fp64_oracle(zc, oracle, prec, tol):
+    """The headline circuit family at its full depth (40 layers of u3 on every
+    qubit + matching CX), 22 qubits, fast arithmetic against the FP64 oracle:
+    max |d amp| within the fast-mode tolerance, TVD <= 1e-6 for f64."""
+    p = C.matching_circuit(22, 40, 7).to_program()
+    _, _, sv, _ = oracle.run(p, prec=64, shots=0, statevector=True)
+    r = zc.run(p, shots=0, precision=prec, statevector=True, flags=zc.FLAG_FAST)
+    d = np.abs(r.statevector - sv).max()
+    tvd = 0.5 * np.abs(np.abs(r.statevector) ** 2 - np.abs(sv) ** 2).sum()
+    assert d < tol, (prec, d)
+    if prec == 64:
+        assert tvd < 1e-6, tvd
+
+
+def test_qft_22q_exact_and_fast(zc, oracle):
+    """QFT with the final SWAP network at 22 qubits: exact mode bit-identical
+    to the oracle (state and counts); fast f64 within 1e-12 of the DFT of the
+    prepared basis state."""
+    c, x = C.qft_circuit(22, 9)
+    p = c.to_program()
+    ref, _, sv, _ = oracle.run(p, prec=64, shots=8192, seed=4, statevector=True)
+    ex = zc.run(p, shots=8192, seed=4, precision=64, statevector=True, flags=zc.FLAG_EXACT)
+    assert bits_equal(ex.statevector, sv)
+    assert ex.counts == ref
+    fa = zc.run(p, shots=0, precision=64, statevector=True, flags=zc.FLAG_FAST)
+    dim = 1 << 22
+    want = np.exp(2j * np.pi * x * np.arange(dim) / dim) / np.sqrt(dim)
+    assert np.abs(fa.statevector - want).max() < 1e-12

@@ -206,27 +206,31 @@ def trajectories(peak_gbs) -> Dict[str, object]:
 
 def gate_mix_tc(peak_gbs, tf32_tflops=None, qubits=28) -> Dict[str, object]:
     """28 qubits, depth 60, gates per slot from {H, S, T, RX/RY/RZ, CX, CZ,
-    SWAP} with probabilities {.15, .1, .1, .3, .25, .05, .05}: unfused f32
-    sweeps and k = 5, 6, 7 blocks as 3xTF32 tensor-core GEMMs, each against
-    the f64 run (fast f64: within 1e-12 of exact, far below the f32 errors
-    measured here). Device times from the in-library profiler."""
+    SWAP} with probabilities {.15, .1, .1, .3, .25, .05, .05}: f64 sweeps in
+    double-float (the variant that meets TVD <= 1e-6), unfused f32 sweeps and
+    k = 5, 6, 7 blocks as 3xTF32 tensor-core GEMMs, each against the exact
+    f64 run (zeno's arithmetic, bit-identical to the FP64 oracle in the
+    parity tests). Device times from the in-library profiler."""
     n = qubits
     p = C.mixed_circuit(n, 60, 7).to_program()
     prog1 = zb.compile(p, 1)
-    ref = zb.run(p, shots=0, seed=1, precision=64, flags=zb.FLAG_FAST, statevector=True, program=prog1).statevector
+    t0 = time.perf_counter()
+    ref = zb.run(p, shots=0, seed=1, precision=64, flags=zb.FLAG_EXACT, statevector=True, program=prog1).statevector
     S = 2.0 ** n * 8
-    out = {"workload": "%dq depth-60 gate mix" % n, "rows": []}
-    variants = [("f32 sweeps (fusion 1, FMA)", prog1, zb.FLAG_FAST, None)]
+    out = {"workload": "%dq depth-60 gate mix" % n, "exact_f64_seconds_with_statevector": time.perf_counter() - t0,
+           "rows": []}
+    variants = [("f64 sweeps (fusion 1, double-float on the FP32 pipe)", prog1, zb.FLAG_FAST, None, 64),
+                ("f32 sweeps (fusion 1, FMA)", prog1, zb.FLAG_FAST, None, 32)]
     for k in (5, 6, 7):
         variants.append(("f32 k=%d blocks on tcgen05 (3xTF32, FP32 accumulation)" % k, zb.compile(p, k),
-                         zb.FLAG_FAST | zb.FLAG_TENSOR, k))
-    for name, prog, flags, k in variants:
-        sv = zb.run(p, shots=0, seed=1, precision=32, flags=flags, statevector=True, program=prog).statevector
+                         zb.FLAG_FAST | zb.FLAG_TENSOR, k, 32))
+    for name, prog, flags, k, prec in variants:
+        sv = zb.run(p, shots=0, seed=1, precision=prec, flags=flags, statevector=True, program=prog).statevector
         acc = _accuracy(sv, ref)
         del sv
-        d = device_profile(n, 32, flags, prog, 1, 1, peak_gbs)
+        d = device_profile(n, prec, flags, prog, 1, 1, peak_gbs)
         row = {"variant": name, "ops": len(prog.ops), "device_ms": d["device_ms"], "kernels": d["kernels"],
-               **{k2 + "_vs_f64": v for k2, v in acc.items()}}
+               **{k2 + "_vs_f64": v for k2, v in acc.items()}, "meets_tvd_1e-6": acc["tvd"] <= 1e-6}
         if k is not None:
             blocks = [op for op in prog.ops if op.kind == zb.OP_UNITARY and len(op.qubits) >= 4]
             flops = sum(8.0 * 2.0 ** (n + len(op.qubits)) for op in blocks)

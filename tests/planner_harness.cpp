@@ -103,10 +103,10 @@ static bool apply_plan(std::vector<cd> &s, const zc::SweepPlan &plan, int prec, 
                     if (df) {  // (re hi, re lo, im hi, im lo)
                         const float *e = (const float *)t + 4 * j;
                         tab[j] = cd((double)e[0] + (double)e[1], (double)e[2] + (double)e[3]);
-                    } else if (prec == 64) {
-                        tab[j] = cd(((const double *)t)[j], ((const double *)t)[dim + j]);
+                    } else if (prec == 64) {  // (re, im) pairs
+                        tab[j] = cd(((const double *)t)[2 * j], ((const double *)t)[2 * j + 1]);
                     } else {
-                        tab[j] = cd(((const float *)t)[j], ((const float *)t)[dim + j]);
+                        tab[j] = cd(((const float *)t)[2 * j], ((const float *)t)[2 * j + 1]);
                     }
                 }
                 apply_diag(s, sup, tab);

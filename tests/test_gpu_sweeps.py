@@ -252,8 +252,9 @@ def test_fast_mode_deep_circuit_vs_fp64_oracle(zc, oracle, prec, tol):
 
 def test_qft_22q_exact_and_fast(zc, oracle):
     """QFT with the final SWAP network at 22 qubits: exact mode bit-identical
-    to the oracle (state and counts); fast f64 within 1e-12 of the DFT of the
-    prepared basis state."""
+    to the oracle (state and counts); fast f64 within 1e-12 of the oracle's
+    FP64 state. Both sit within a few 1e-12 of the DFT of the prepared basis
+    state (253 controlled phases with rounded cos/sin accumulate that)."""
     c, x = C.qft_circuit(22, 9)
     p = c.to_program()
     ref, _, sv, _ = oracle.run(p, prec=64, shots=8192, seed=4, statevector=True)
@@ -261,6 +262,7 @@ def test_qft_22q_exact_and_fast(zc, oracle):
     assert bits_equal(ex.statevector, sv)
     assert ex.counts == ref
     fa = zc.run(p, shots=0, precision=64, statevector=True, flags=zc.FLAG_FAST)
+    assert np.abs(fa.statevector - sv).max() < 1e-12
     dim = 1 << 22
     want = np.exp(2j * np.pi * x * np.arange(dim) / dim) / np.sqrt(dim)
-    assert np.abs(fa.statevector - want).max() < 1e-12
+    assert np.abs(sv - want).max() < 1e-11 and np.abs(fa.statevector - want).max() < 1e-11

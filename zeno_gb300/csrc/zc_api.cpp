@@ -411,12 +411,12 @@ size_t plan_sweep(uint32_t n, int prec, bool ex, uint32_t L, uint32_t Hcap, cons
                     e[1] = (float)(xr - (double)e[0]);
                     e[2] = (float)xi;
                     e[3] = (float)(xi - (double)e[2]);
-                } else if (es == 8) {
-                    ((double *)(tables.data() + off))[j] = xr;
-                    ((double *)(tables.data() + off))[dim + j] = xi;
+                } else if (es == 8) {  // (re, im) pairs: one 16-byte load per entry
+                    ((double *)(tables.data() + off))[2 * j] = xr;
+                    ((double *)(tables.data() + off))[2 * j + 1] = xi;
                 } else {
-                    ((float *)(tables.data() + off))[j] = (float)xr;
-                    ((float *)(tables.data() + off))[dim + j] = (float)xi;
+                    ((float *)(tables.data() + off))[2 * j] = (float)xr;
+                    ((float *)(tables.data() + off))[2 * j + 1] = (float)xi;
                 }
             }
             m.table = off;

@@ -29,6 +29,14 @@ namespace {
 constexpr int kSweepThreads = 256;
 constexpr int kSweepCtasPerSm = 3;
 constexpr uint32_t kJlutHigh = 1u << (13 - 8);  // tile index values above the low byte (tiles <= 2^13)
+constexpr uint32_t kJlutLen = 256 + kJlutHigh;
+// Sweeps without register passes (f32 and exact f64) keep the index tables
+// of their first kJobLuts table diagonals for the whole job, in the shared
+// memory the pass descriptors take in double-float sweeps; further table
+// diagonals build theirs per tile. A table diagonal's `b` field (in the
+// CTA's copy of the micro-ops) names its job table, or kNoJobLut.
+constexpr int kJobLuts = 5;
+constexpr uint32_t kNoJobLut = 0xffffffffu;
 
 // Global index of the first element of tile t: the tile number fills the
 // non-local positions above the L low bits.
@@ -342,7 +350,8 @@ __device__ void run_pass_any(const GroupInfo &gi, float2 *sr, float2 *si, const 
 // fuse_in / fuse_out: its first / last pass converts the tile.
 template <typename T, int A, typename R>
 __device__ void apply_ops(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *coef, int nops, uint64_t base,
-                          uint32_t size, const char *tables, uint32_t *bad, uint16_t *jlut, const GroupInfo *gis,
+                          uint32_t size, const char *tables, uint32_t *bad, uint16_t *jlut, const uint16_t *job_luts,
+                          const GroupInfo *gis,
                           int fuse_in = 0, int fuse_out = 0) {
     const int tid = threadIdx.x, nt = blockDim.x;
     for (int o = 0; o < nops; o++) {
@@ -453,21 +462,29 @@ __device__ void apply_ops(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *c
             for (; v < size; v += nt) scl(v, sr[v], si[v]);
         } else if (op.kind == MOP_DK) {
             const uint32_t jo = jouter(op, base);
-            const T *dre = reinterpret_cast<const T *>(tables + op.table);
-            const T *dim_ = dre + (1u << op.k);
-            const float4 *dtab = reinterpret_cast<const float4 *>(tables + op.table);  // double-float entries
+            // (re, im) pairs of T, or double-float (re hi, re lo, im hi, im lo)
+            using P2 = typename std::conditional<sizeof(T) == 8, double2, float2>::type;
+            const P2 *ptab = reinterpret_cast<const P2 *>(tables + op.table);
+            const float4 *dtab = reinterpret_cast<const float4 *>(tables + op.table);
             // table index of element v = jo | lut[v & 255] | lut[256 + (v >> 8)]:
-            // the op's local bits gathered once per op instead of per element
-            for (uint32_t x = tid; x < 256 + kJlutHigh; x += nt)
-                jlut[x] = (uint16_t)jgather<R>(op, 0u, x < 256 ? x : (x - 256) << 8);
-            __syncthreads();
+            // the op's local bits gathered once per job (or once per tile)
+            // instead of per element
+            const uint16_t *lut = jlut;
+            if (op.b != kNoJobLut) {
+                lut = job_luts + (size_t)op.b * kJlutLen;
+            } else {
+                for (uint32_t x = tid; x < kJlutLen; x += nt)
+                    jlut[x] = (uint16_t)jgather<R>(op, 0u, x < 256 ? x : (x - 256) << 8);
+                __syncthreads();
+            }
             // W: the table entry (T re, T im; or one float4 of double-float pairs)
             using W = typename std::conditional<A == AR_DF, float4, T>::type;
             auto load_w = [&](uint32_t j, W &wr, W &wi) {
                 if constexpr (A == AR_DF) wr = __ldg(dtab + j);
                 else {
-                    wr = __ldg(dre + j);
-                    wi = __ldg(dim_ + j);
+                    const P2 w = __ldg(ptab + j);
+                    wr = w.x;
+                    wi = w.y;
                 }
             };
             auto scl = [&](const W &wr, const W &wi, R &xr, R &xi) {
@@ -481,7 +498,7 @@ __device__ void apply_ops(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *c
 #pragma unroll
                 for (int k = 0; k < 4; k++) {
                     const uint32_t vk = v + k * nt;
-                    const uint32_t j = jo | jlut[vk & 255u] | jlut[256 + (vk >> 8)];
+                    const uint32_t j = jo | lut[vk & 255u] | lut[256 + (vk >> 8)];
                     load_w(j, wr[k], wi[k]);
                     xr[k] = sr[vk];
                     xi[k] = si[vk];
@@ -494,7 +511,7 @@ __device__ void apply_ops(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *c
                 }
             }
             for (; v < size; v += nt) {
-                const uint32_t j = jo | jlut[v & 255u] | jlut[256 + (v >> 8)];
+                const uint32_t j = jo | lut[v & 255u] | lut[256 + (v >> 8)];
                 W wr, wi;
                 load_w(j, wr, wi);
                 scl(wr, wi, sr[v], si[v]);
@@ -520,10 +537,13 @@ struct SweepSmem {
     int has_arith;
     int fail;
     uint32_t fail_tile, done_tiles, bad;
-    uint16_t jlut[256 + kJlutHigh];  // diagonal index tables of the current DK op
-    GroupInfo gi[kMaxMicroOps];      // register passes (double-float sweeps)
-    int fuse_in, fuse_out;           // the first / last pass converts the tile
+    uint16_t jlut[kJlutLen];  // diagonal index tables of the current DK op
+    // register passes (double-float sweeps), or the job's diagonal index tables
+    typename std::conditional<A == AR_DF, GroupInfo[kMaxMicroOps], uint16_t[kJobLuts * kJlutLen]>::type gi;
+    int fuse_in, fuse_out;  // the first / last pass converts the tile
 };
+static_assert(sizeof(uint16_t[kJobLuts * kJlutLen]) <= sizeof(GroupInfo[kMaxMicroOps]),
+              "job index tables fit where the pass descriptors go");
 
 // All threads: make (gops, nops, L, H, hpos) the CTA's current job.
 template <typename T, int A>
@@ -562,15 +582,28 @@ __device__ void load_job(SweepSmem<T, A> &c, const MicroOp *gops, int nops, uint
         }
     }
     if (tid == 0) {
-        int ar = 0;
-        for (int o = 0; o < nops; o++)
+        int ar = 0, nlut = 0;
+        for (int o = 0; o < nops; o++) {
             ar |= c.ops[o].kind != MOP_CX && c.ops[o].kind != MOP_SWAP;
+            if (c.ops[o].kind == MOP_DK)
+                c.ops[o].b = A != AR_DF && nlut < kJobLuts ? (uint32_t)nlut++ : kNoJobLut;
+        }
         c.has_arith = ar;
         c.fuse_in = c.fuse_out = 0;
         if constexpr (A == AR_DF)
             plan_passes(c.ops, nops, L + H, fold, max_group_of<T, A>(), c.gi, &c.bad, &c.fuse_in, &c.fuse_out);
     }
     __syncthreads();
+    if constexpr (A != AR_DF) {  // the job's diagonal index tables, once per job
+        for (int o = 0; o < nops; o++) {
+            const OpHead &op = c.ops[o];
+            if (op.kind != MOP_DK || op.b == kNoJobLut) continue;
+            uint16_t *lut = c.gi + (size_t)op.b * kJlutLen;
+            for (uint32_t x = tid; x < kJlutLen; x += blockDim.x)
+                lut[x] = (uint16_t)jgather<T>(op, 0u, x < 256 ? x : (x - 256) << 8);
+        }
+        __syncthreads();
+    }
 }
 
 // Global offset of row r of a tile: bit j of r at qubit hpos[j].
@@ -622,7 +655,8 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
             }
             __syncthreads();
         }
-        apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut, c.gi, fuse_in,
+        apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut, nullptr, c.gi,
+                                fuse_in,
                                 fuse_out);
         if (c.has_arith && !fuse_out) {  // register passes leave pairs unnormalised
             for (uint32_t v = tid; v < size; v += blockDim.x) {
@@ -646,7 +680,7 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
             }
         }
     } else {
-        apply_ops<T, A, T>(sre, sim, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut, c.gi);
+        apply_ops<T, A, T>(sre, sim, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut, c.gi, nullptr);
     }
     fence_async_smem();
     __syncthreads();

@@ -25,9 +25,9 @@ struct SweepGeom {
 
 // One op inside a sweep, operands as local bit indices (0..L+H) or
 // kOuterFlag | global qubit. U1: a = bit, m = 2x2 row-major (re, im);
-// D1: a = bit, m[0..4) = d0, d1; DK: k, loc[], table = byte offset of
-// [re(2^k) | im(2^k)] in the sweep's table block (for double-float sweeps
-// of f64 states: 2^k entries of (re hi, re lo, im hi, im lo) floats);
+// D1: a = bit, m[0..4) = d0, d1; DK: k, loc[], table = byte offset of 2^k
+// (re, im) pairs in the sweep's table block (for double-float sweeps of f64
+// states: 2^k entries of (re hi, re lo, im hi, im lo) floats);
 // CX: a = control, b = target (local); SWAP: a, b local; R1: a = bit,
 // m[0..4) = real 2x2 r00 r01 r10 r11; RT: a = bit, m[0] = t, b = flip:
 // [[1, -t], [t, 1]], then (flip) the pair's two amplitudes trade places.

@@ -285,10 +285,10 @@ size_t plan_sweep(uint32_t n, int prec, bool ex, uint32_t L, uint32_t Hcap, cons
     // Order of the micro-ops. Exact mode keeps program order (reordering two
     // gates changes the rounding). Fast mode lets ops on disjoint qubits
     // commute: one-qubit ops on distinct qubits are emitted back to back, in
-    // runs the size of the kernel's register groups (three for f32 states
-    // and for the rotations of lowered f64 sweeps, else two), so the kernel
-    // applies each run in one register pass.
-    const size_t run_cap = prec == 64 && !df_lowering ? 2 : 3;
+    // runs the size of the kernel's register groups (three for the rotations
+    // of lowered f64 sweeps, else two: f32 groups of two move element pairs
+    // as 8-byte vectors), so the kernel applies each run in one register pass.
+    const size_t run_cap = prec == 32 ? 2 : (prec == 64 && !df_lowering ? 2 : 3);
     const bool df = df_lowering;
     std::vector<LoweredOp> low;
     for (;;) {

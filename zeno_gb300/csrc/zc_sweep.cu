@@ -55,11 +55,54 @@ __device__ __forceinline__ void swap_slots(T *sr, T *si, uint32_t v0, uint32_t v
     si[v1] = x;
 }
 
+// Swap 16-byte vectors of slots (VW consecutive elements) at v0 <-> v1.
+__device__ __forceinline__ void swap_vec(void *sr, void *si, uint32_t v0, uint32_t v1) {
+    uint4 *r = reinterpret_cast<uint4 *>(sr), *i = reinterpret_cast<uint4 *>(si);
+    const uint4 a = r[v0], b = r[v1], c = i[v0], d = i[v1];
+    r[v0] = b;
+    r[v1] = a;
+    i[v0] = d;
+    i[v1] = c;
+}
+
+__device__ __forceinline__ uint32_t insert_zero32(uint32_t v, uint32_t b) {
+    return ((v >> b) << (b + 1)) | (v & ((1u << b) - 1));
+}
+
 // Permutation micro-ops (CX, SWAP) move raw slots, so they serve every
-// arithmetic policy and representation.
+// arithmetic policy and representation. When none of the op's bits is among
+// the lowest log2(VW), the VW consecutive slots of a 16-byte vector move
+// together: one vector load and store per VW elements.
 template <typename T>
 __device__ void apply_perm(T *sr, T *si, const OpHead &op, uint64_t base, uint32_t size) {
     const int tid = threadIdx.x, nt = blockDim.x;
+    constexpr uint32_t VW = 16 / sizeof(T), VB = VW == 4 ? 2 : 1;  // elements per vector, log2
+    const uint32_t nv = size / VW;                                   // vectors in the tile
+    if (op.kind == MOP_CX && !(op.a & kOuterFlag) && min(op.a, op.b) >= VB) {
+        const uint32_t c = op.a - VB, t = op.b - VB, lo = min(c, t), hi = max(c, t);
+        for (uint32_t p = tid; p < nv / 4; p += nt) {
+            const uint32_t v0 = insert_zero32(insert_zero32(p, lo), hi) | (1u << c);
+            swap_vec(sr, si, v0, v0 | (1u << t));
+        }
+        return;
+    }
+    if (op.kind == MOP_CX && (op.a & kOuterFlag) && op.b >= VB) {
+        if (!((base >> (op.a & ~kOuterFlag)) & 1)) return;
+        const uint32_t t = op.b - VB;
+        for (uint32_t p = tid; p < nv / 2; p += nt) {
+            const uint32_t v0 = insert_zero32(p, t);
+            swap_vec(sr, si, v0, v0 | (1u << t));
+        }
+        return;
+    }
+    if (op.kind == MOP_SWAP && min(op.a, op.b) >= VB) {
+        const uint32_t lo = min(op.a, op.b) - VB, hi = max(op.a, op.b) - VB;
+        for (uint32_t p = tid; p < nv / 4; p += nt) {
+            const uint32_t v = insert_zero32(insert_zero32(p, lo), hi);
+            swap_vec(sr, si, v | (1u << lo), v | (1u << hi));
+        }
+        return;
+    }
     if (op.kind == MOP_CX) {
         const uint32_t t = op.b;
         if (op.a & kOuterFlag) {
@@ -96,10 +139,12 @@ struct OpCoef {
 };
 
 // The kernel's register group size: f64 states outside FMA mode spill at the
-// 80-register cap with more than two general ops (rotations: three).
+// 80-register cap with more than two general ops (rotations: three); f32
+// states run groups of two as 8-byte vectors of element pairs (measured
+// faster than scalar groups of three, which spill as vectors).
 template <typename T, int A>
 __host__ __device__ constexpr int max_group_of() {
-    return sizeof(T) == 8 && A != AR_FMA ? 2 : 3;
+    return sizeof(T) == 4 ? 2 : (A != AR_FMA ? 2 : 3);
 }
 
 template <typename R>
@@ -117,19 +162,69 @@ __device__ __forceinline__ uint32_t jouter(const OpHead &op, uint64_t base) {
     return jo;
 }
 
-// Apply G consecutive one-qubit micro-ops (U1, R1 or RT; only RT when
-// ROT_ONLY; ops[o..o+G), distinct tile bits) to register-held groups of 2^G
-// elements: each gate updates the same pairs with the same arithmetic, in the
-// same order, as one op at a time. The pair swaps of flipped RT ops commute
-// with the group's other gates (other bits), so they all happen at the store:
-// element e goes to the slot of e ^ flips.
-template <typename T, int A, typename R, int G, bool ROT_ONLY = false>
-__device__ void apply_u1_group(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *coef, int o, uint32_t size,
-                               uint32_t *bad) {
-    constexpr int E = 1 << G;
-    uint32_t bits[G], sorted[G];
+// The arithmetic of G consecutive one-qubit micro-ops (U1, R1 or RT; only RT
+// when ROT_ONLY; ops[o..o+G), distinct tile bits) on a register-held group
+// of 2^G elements: element e sits at the slot of the group bits selected by
+// e. Each gate updates the same pairs with the same arithmetic, in the same
+// order, as one op at a time.
+// NE: elements held (a multiple of 2^G: several independent groups side by
+// side, element e of group h at index h * 2^G + e; each gate's coefficients
+// are read once for all of them).
+template <typename T, int A, typename R, int G, bool ROT_ONLY, int NE = (1 << G)>
+__device__ __forceinline__ void group_math(const OpHead *ops, const OpCoef<T, A> *coef, int o, R *xr, R *xi) {
+    constexpr int E = NE;
 #pragma unroll
-    for (int g = 0; g < G; g++) bits[g] = sorted[g] = ops[o + g].a;
+    for (int g = 0; g < G; g++) {
+        if (ROT_ONLY || ops[o + g].kind == MOP_RT) {
+            const R t = coef[o + g].v[0];
+#pragma unroll
+            for (int e = 0; e < E; e++)
+                if (!((e >> g) & 1)) {
+                    if constexpr (A == AR_DF)
+                        pair_update_rot_df(t, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                    else
+                        pair_update_rot<T>(t, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                }
+        } else if (ops[o + g].kind == MOP_R1) {
+            R r[4];
+#pragma unroll
+            for (int i = 0; i < 4; i++) r[i] = coef[o + g].v[i];
+#pragma unroll
+            for (int e = 0; e < E; e++)
+                if (!((e >> g) & 1)) {
+                    if constexpr (A == AR_DF)
+                        pair_update_rdf(r, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                    else
+                        pair_update_real<T>(r, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                }
+        } else if constexpr (A == AR_DF) {
+            MatDF m;
+#pragma unroll
+            for (int i = 0; i < 8; i++) m.v[i] = coef[o + g].v[i];
+#pragma unroll
+            for (int e = 0; e < E; e++)
+                if (!((e >> g) & 1)) pair_update_df(m, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+        } else {
+            Mat2<T> m;
+#pragma unroll
+            for (int i = 0; i < 8; i++) m.v[i] = coef[o + g].v[i];
+#pragma unroll
+            for (int e = 0; e < E; e++)
+                if (!((e >> g) & 1))
+                    pair_update<T, A == AR_EXACT>(m, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+        }
+    }
+}
+
+// The group's tile bits (bits: op order; sorted: ascending), the pattern of
+// flipped RT ops and a range check. Returns false (and records the bad bit)
+// when a bit lies outside the tile; `shift` counts the low bits a vector of
+// consecutive elements covers (the bits are then in vector units).
+template <int G>
+__device__ __forceinline__ bool group_bits(const OpHead *ops, int o, uint32_t size, uint32_t shift, uint32_t *bits,
+                                           uint32_t *sorted, uint32_t &fmask, uint32_t *bad) {
+#pragma unroll
+    for (int g = 0; g < G; g++) bits[g] = sorted[g] = ops[o + g].a - shift;
 #pragma unroll
     for (int i = 1; i < G; i++)
 #pragma unroll
@@ -139,19 +234,33 @@ __device__ void apply_u1_group(R *sr, R *si, const OpHead *ops, const OpCoef<T, 
                 sorted[j] = sorted[j - 1];
                 sorted[j - 1] = x;
             }
-    uint32_t fmask = 0, bad_bit = 0;
+    uint32_t bad_bit = 0;
+    fmask = 0;
 #pragma unroll
     for (int g = 0; g < G; g++) {
         if (ops[o + g].kind == MOP_RT && ops[o + g].b) fmask |= 1u << bits[g];
-        if ((1u << bits[g]) >= size) bad_bit = bits[g];
+        if ((1u << ops[o + g].a) >= size) bad_bit = ops[o + g].a;
     }
     // every slot is inside the tile when the bits are (v < size / 2^G with
     // G zero bits inserted below log2(size)); a bad bit is recorded and the
     // group skipped
     if (bad_bit) {
         if (threadIdx.x == 0) *bad = bad_bit | 0x80000000u;
-        return;
+        return false;
     }
+    return true;
+}
+
+// Apply G consecutive one-qubit micro-ops to register-held groups of 2^G
+// elements (group_math). The pair swaps of flipped RT ops commute with the
+// group's other gates (other bits), so they all happen at the store: element
+// e goes to the slot of e ^ flips.
+template <typename T, int A, typename R, int G, bool ROT_ONLY = false>
+__device__ void apply_u1_group(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *coef, int o, uint32_t size,
+                               uint32_t *bad) {
+    constexpr int E = 1 << G;
+    uint32_t bits[G], sorted[G], fmask;
+    if (!group_bits<G>(ops, o, size, 0u, bits, sorted, fmask, bad)) return;
     for (uint32_t p = threadIdx.x; p < size / E; p += blockDim.x) {
         uint32_t v = p;
 #pragma unroll
@@ -173,53 +282,56 @@ __device__ void apply_u1_group(R *sr, R *si, const OpHead *ops, const OpCoef<T, 
             xr[e] = sr[w];
             xi[e] = si[w];
         }
-#pragma unroll
-        for (int g = 0; g < G; g++) {
-            if (ROT_ONLY || ops[o + g].kind == MOP_RT) {
-                const R t = coef[o + g].v[0];
-#pragma unroll
-                for (int e = 0; e < E; e++)
-                    if (!((e >> g) & 1)) {
-                        if constexpr (A == AR_DF)
-                            pair_update_rot_df(t, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
-                        else
-                            pair_update_rot<T>(t, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
-                    }
-            } else if (ops[o + g].kind == MOP_R1) {
-                R r[4];
-#pragma unroll
-                for (int i = 0; i < 4; i++) r[i] = coef[o + g].v[i];
-#pragma unroll
-                for (int e = 0; e < E; e++)
-                    if (!((e >> g) & 1)) {
-                        if constexpr (A == AR_DF)
-                            pair_update_rdf(r, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
-                        else
-                            pair_update_real<T>(r, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
-                    }
-            } else if constexpr (A == AR_DF) {
-                MatDF m;
-#pragma unroll
-                for (int i = 0; i < 8; i++) m.v[i] = coef[o + g].v[i];
-#pragma unroll
-                for (int e = 0; e < E; e++)
-                    if (!((e >> g) & 1)) pair_update_df(m, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
-            } else {
-                Mat2<T> m;
-#pragma unroll
-                for (int i = 0; i < 8; i++) m.v[i] = coef[o + g].v[i];
-#pragma unroll
-                for (int e = 0; e < E; e++)
-                    if (!((e >> g) & 1))
-                        pair_update<T, A == AR_EXACT>(m, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
-            }
-        }
+        group_math<T, A, R, G, ROT_ONLY>(ops, coef, o, xr, xi);
         const uint32_t vs = v ^ fmask;
 #pragma unroll
         for (int e = 0; e < E; e++) {
             const uint32_t w = slot(vs, (uint32_t)e);
             sr[w] = xr[e];
             si[w] = xi[e];
+        }
+    }
+}
+
+// The same for 4-byte elements when no group bit is bit 0: each thread
+// moves element pairs (2m, 2m + 1) as one 8-byte vector, so a group of 2^G
+// vectors carries two independent element groups (the vector's two lanes)
+// with half the loads, stores and index arithmetic per element.
+template <typename T, int A, int G, bool ROT_ONLY = false>
+__device__ void apply_u1_group_v2(float *sr, float *si, const OpHead *ops, const OpCoef<T, A> *coef, int o,
+                                  uint32_t size, uint32_t *bad) {
+    constexpr int E = 1 << G;
+    uint32_t bits[G], sorted[G], fmask;
+    if (!group_bits<G>(ops, o, size, 1u, bits, sorted, fmask, bad)) return;
+    float2 *vr = reinterpret_cast<float2 *>(sr), *vi = reinterpret_cast<float2 *>(si);
+    for (uint32_t p = threadIdx.x; p < size / 2 / E; p += blockDim.x) {
+        uint32_t v = p;
+#pragma unroll
+        for (int g = 0; g < G; g++) v = ((v >> sorted[g]) << (sorted[g] + 1)) | (v & ((1u << sorted[g]) - 1));
+        auto slot = [&](uint32_t base_v, uint32_t e) {
+            uint32_t w = base_v;
+#pragma unroll
+            for (int g = 0; g < G; g++)
+                if ((e >> g) & 1u) w ^= 1u << bits[g];
+            return w;
+        };
+        float xr[2 * E], xi[2 * E];  // lane 0 (even element) at e, lane 1 at E + e
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            const uint32_t w = slot(v, (uint32_t)e);
+            const float2 a = vr[w], b = vi[w];
+            xr[e] = a.x;
+            xr[E + e] = a.y;
+            xi[e] = b.x;
+            xi[E + e] = b.y;
+        }
+        group_math<T, A, float, G, ROT_ONLY, 2 * E>(ops, coef, o, xr, xi);
+        const uint32_t vs = v ^ fmask;
+#pragma unroll
+        for (int e = 0; e < E; e++) {
+            const uint32_t w = slot(vs, (uint32_t)e);
+            vr[w] = make_float2(xr[e], xr[E + e]);
+            vi[w] = make_float2(xi[e], xi[E + e]);
         }
     }
 }
@@ -378,6 +490,17 @@ __device__ void apply_ops(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *c
             constexpr int kMaxGroup = max_group_of<T, A>();
             bool rot3;
             const int g = group_at(ops, o, nops, kMaxGroup, &rot3);
+            if constexpr (sizeof(R) == 4) {  // 4-byte elements: pairs of them as 8-byte vectors
+                bool vec = g <= 2;
+                for (int h = 0; h < g; h++) vec &= ops[o + h].a >= 1u;
+                if (vec) {
+                    if (g == 2) apply_u1_group_v2<T, A, 2>(sr, si, ops, coef, o, size, bad);
+                    else apply_u1_group_v2<T, A, 1>(sr, si, ops, coef, o, size, bad);
+                    o += g - 1;
+                    __syncthreads();
+                    continue;
+                }
+            }
             if (rot3) {
                 apply_u1_group<T, A, R, 3, true>(sr, si, ops, coef, o, size, bad);
                 o += 2;
@@ -444,22 +567,34 @@ __device__ void apply_ops(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *c
                 if constexpr (A == AR_DF) cscale_df(coef[o].v[one ? 2 : 0], coef[o].v[one ? 3 : 1], xr, xi);
                 else cscale<T, A == AR_EXACT>(coef[o].v[one ? 2 : 0], coef[o].v[one ? 3 : 1], xr, xi);
             };
-            uint32_t v = tid;
-            for (; v + 3u * nt < size; v += 4u * nt) {
-                R xr[4], xi[4];
+            if constexpr (sizeof(R) == 4) {  // four consecutive elements per 16-byte vector
+                float4 *vr = reinterpret_cast<float4 *>(sr), *vi = reinterpret_cast<float4 *>(si);
+                for (uint32_t q = tid; q < size / 4; q += nt) {
+                    const float4 a = vr[q], b = vi[q];
+                    R xr[4] = {a.x, a.y, a.z, a.w}, xi[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    xr[k] = sr[v + k * nt];
-                    xi[k] = si[v + k * nt];
+                    for (int k = 0; k < 4; k++) scl(4 * q + k, xr[k], xi[k]);
+                    vr[q] = make_float4(xr[0], xr[1], xr[2], xr[3]);
+                    vi[q] = make_float4(xi[0], xi[1], xi[2], xi[3]);
                 }
+            } else {
+                uint32_t v = tid;
+                for (; v + 3u * nt < size; v += 4u * nt) {
+                    R xr[4], xi[4];
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    scl(v + k * nt, xr[k], xi[k]);
-                    sr[v + k * nt] = xr[k];
-                    si[v + k * nt] = xi[k];
+                    for (int k = 0; k < 4; k++) {
+                        xr[k] = sr[v + k * nt];
+                        xi[k] = si[v + k * nt];
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        scl(v + k * nt, xr[k], xi[k]);
+                        sr[v + k * nt] = xr[k];
+                        si[v + k * nt] = xi[k];
+                    }
                 }
+                for (; v < size; v += nt) scl(v, sr[v], si[v]);
             }
-            for (; v < size; v += nt) scl(v, sr[v], si[v]);
         } else if (op.kind == MOP_DK) {
             const uint32_t jo = jouter(op, base);
             // (re, im) pairs of T, or double-float (re hi, re lo, im hi, im lo)
@@ -491,30 +626,46 @@ __device__ void apply_ops(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *c
                 if constexpr (A == AR_DF) cscale_df(make_float2(wr.x, wr.y), make_float2(wr.z, wr.w), xr, xi);
                 else cscale<T, A == AR_EXACT>(wr, wi, xr, xi);
             };
-            uint32_t v = tid;
-            for (; v + 3u * nt < size; v += 4u * nt) {
-                R xr[4], xi[4];
-                W wr[4], wi[4];
+            if constexpr (sizeof(R) == 4) {  // four consecutive elements per 16-byte vector
+                float4 *vr = reinterpret_cast<float4 *>(sr), *vi = reinterpret_cast<float4 *>(si);
+                for (uint32_t q = tid; q < size / 4; q += nt) {
+                    const uint32_t v0 = 4 * q, jh = jo | lut[256 + (v0 >> 8)];  // same high bits for all four
+                    W wr[4], wi[4];
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    const uint32_t vk = v + k * nt;
-                    const uint32_t j = jo | lut[vk & 255u] | lut[256 + (vk >> 8)];
-                    load_w(j, wr[k], wi[k]);
-                    xr[k] = sr[vk];
-                    xi[k] = si[vk];
-                }
+                    for (int k = 0; k < 4; k++) load_w(jh | lut[(v0 & 255u) + k], wr[k], wi[k]);
+                    const float4 a = vr[q], b = vi[q];
+                    R xr[4] = {a.x, a.y, a.z, a.w}, xi[4] = {b.x, b.y, b.z, b.w};
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
-                    scl(wr[k], wi[k], xr[k], xi[k]);
-                    sr[v + k * nt] = xr[k];
-                    si[v + k * nt] = xi[k];
+                    for (int k = 0; k < 4; k++) scl(wr[k], wi[k], xr[k], xi[k]);
+                    vr[q] = make_float4(xr[0], xr[1], xr[2], xr[3]);
+                    vi[q] = make_float4(xi[0], xi[1], xi[2], xi[3]);
                 }
-            }
-            for (; v < size; v += nt) {
-                const uint32_t j = jo | lut[v & 255u] | lut[256 + (v >> 8)];
-                W wr, wi;
-                load_w(j, wr, wi);
-                scl(wr, wi, sr[v], si[v]);
+            } else {
+                uint32_t v = tid;
+                for (; v + 3u * nt < size; v += 4u * nt) {
+                    R xr[4], xi[4];
+                    W wr[4], wi[4];
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        const uint32_t vk = v + k * nt;
+                        const uint32_t j = jo | lut[vk & 255u] | lut[256 + (vk >> 8)];
+                        load_w(j, wr[k], wi[k]);
+                        xr[k] = sr[vk];
+                        xi[k] = si[vk];
+                    }
+#pragma unroll
+                    for (int k = 0; k < 4; k++) {
+                        scl(wr[k], wi[k], xr[k], xi[k]);
+                        sr[v + k * nt] = xr[k];
+                        si[v + k * nt] = xi[k];
+                    }
+                }
+                for (; v < size; v += nt) {
+                    const uint32_t j = jo | lut[v & 255u] | lut[256 + (v >> 8)];
+                    W wr, wi;
+                    load_w(j, wr, wi);
+                    scl(wr, wi, sr[v], si[v]);
+                }
             }
         } else {
             apply_perm(sr, si, op, base, size);

@@ -8,6 +8,7 @@
 #include <string.h>
 
 #include <algorithm>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -720,6 +721,66 @@ extern "C" int zc_create_ex(uint32_t n, int prec, uint32_t flags, zc_state **out
     return create_state(n, prec, flags, budget, out);
 }
 
+namespace zc {
+namespace {
+
+// A state's buffers that do not depend on its size: stream, parameter ring
+// (pinned host + device), scalar and error words, sampler scratch. Released
+// states hand them to a small per-process cache (at most kKitCache, per
+// device) and new states take them from it, so a run of short-lived states —
+// one zc_run per circuit — does not pay a 32 MiB pinned allocation, a device
+// allocation and their frees every time. The cache holds up to
+// kKitCache x 64 MiB (half pinned host, half device) until the process exits.
+struct Kit {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    Arena arena;
+    double *d_scalar = nullptr, *h_scalar = nullptr;
+    int *d_err = nullptr;
+    double *d_part = nullptr;
+    size_t part_cap = 0;
+    void *d_samp = nullptr;
+    size_t samp_cap = 0;
+};
+constexpr size_t kKitCache = 4;
+std::mutex g_kit_mu;
+std::vector<Kit> g_kits;
+
+void free_kit(Kit &k) {
+    if (k.stream) cudaStreamSynchronize(k.stream);
+    if (k.arena.host) cudaFreeHost(k.arena.host);
+    if (k.arena.dev) cudaFree(k.arena.dev);
+    if (k.d_part) cudaFree(k.d_part);
+    if (k.d_scalar) cudaFree(k.d_scalar);
+    if (k.h_scalar) cudaFreeHost(k.h_scalar);
+    if (k.d_samp) cudaFree(k.d_samp);
+    if (k.d_err) cudaFree(k.d_err);
+    if (k.stream) cudaStreamDestroy(k.stream);
+    k = Kit{};
+}
+
+bool take_kit(int device, Kit *out) {
+    std::lock_guard<std::mutex> lk(g_kit_mu);
+    for (size_t i = 0; i < g_kits.size(); i++)
+        if (g_kits[i].device == device) {
+            *out = g_kits[i];
+            g_kits.erase(g_kits.begin() + (long)i);
+            return true;
+        }
+    return false;
+}
+
+// Returns false when the cache is full (the caller frees the kit).
+bool give_kit(const Kit &k) {
+    std::lock_guard<std::mutex> lk(g_kit_mu);
+    if (g_kits.size() >= kKitCache) return false;
+    g_kits.push_back(k);
+    return true;
+}
+
+}  // namespace
+}  // namespace zc
+
 int zc::create_state(uint32_t n, int prec, uint32_t flags, uint64_t budget, zc_state **out) {
     if (!out) return fail(ZC_ERR_INVALID, "null output handle");
     *out = nullptr;
@@ -749,7 +810,21 @@ int zc::create_state(uint32_t n, int prec, uint32_t flags, uint64_t budget, zc_s
             return r_;                     \
         }                                  \
     } while (0)
-    TRY(cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking));
+    Kit kit;
+    if (take_kit(dev, &kit)) {  // stream, ring, scalars, sampler scratch of a released state
+        st->stream = kit.stream;
+        st->arena = kit.arena;
+        st->arena.head = 0;
+        st->d_scalar = kit.d_scalar;
+        st->h_scalar = kit.h_scalar;
+        st->d_err = kit.d_err;
+        st->d_part = kit.d_part;
+        st->part_cap = kit.part_cap;
+        st->d_samp = kit.d_samp;
+        st->samp_cap = kit.samp_cap;
+    } else {
+        TRY(cudaStreamCreateWithFlags(&st->stream, cudaStreamNonBlocking));
+    }
     e = cudaMalloc(&st->re, bytes);
     if (e == cudaSuccess) e = cudaMalloc(&st->im, bytes);
     if (e != cudaSuccess) {
@@ -758,13 +833,15 @@ int zc::create_state(uint32_t n, int prec, uint32_t flags, uint64_t budget, zc_s
         zc_destroy(st);
         return ZC_ERR_MEMORY;
     }
-    TRY(cudaMallocHost(&st->arena.host, kArenaBytes));
-    TRY(cudaMalloc(&st->arena.dev, kArenaBytes));
-    st->arena.cap = kArenaBytes;
-    TRY(cudaMalloc(&st->d_scalar, sizeof(double)));
-    TRY(cudaMalloc(&st->d_err, kErrWords * sizeof(int)));
+    if (!st->arena.host) {
+        TRY(cudaMallocHost(&st->arena.host, kArenaBytes));
+        TRY(cudaMalloc(&st->arena.dev, kArenaBytes));
+        st->arena.cap = kArenaBytes;
+        TRY(cudaMalloc(&st->d_scalar, sizeof(double)));
+        TRY(cudaMalloc(&st->d_err, kErrWords * sizeof(int)));
+        TRY(cudaMallocHost(&st->h_scalar, sizeof(double)));
+    }
     TRY(cudaMemsetAsync(st->d_err, 0, kErrWords * sizeof(int), st->stream));
-    TRY(cudaMallocHost(&st->h_scalar, sizeof(double)));
 #undef TRY
     rc = launch_reset(st);
     if (rc) {
@@ -779,22 +856,28 @@ extern "C" {
 
 void zc_destroy(zc_state *st) {
     if (!st) return;
-    if (st->stream) cudaStreamSynchronize(st->stream);
+    const bool healthy = !st->stream || cudaStreamSynchronize(st->stream) == cudaSuccess;
     if (st->re) cudaFree(st->re);
     if (st->im) cudaFree(st->im);
-    if (st->arena.host) cudaFreeHost(st->arena.host);
-    if (st->arena.dev) cudaFree(st->arena.dev);
-    if (st->d_part) cudaFree(st->d_part);
-    if (st->d_scalar) cudaFree(st->d_scalar);
-    if (st->h_scalar) cudaFreeHost(st->h_scalar);
-    if (st->d_samp) cudaFree(st->d_samp);
-    if (st->d_err) cudaFree(st->d_err);
     for (auto &r : st->prof_recs) {
         cudaEventDestroy(r.a);
         cudaEventDestroy(r.b);
     }
     for (auto e : st->prof_pool) cudaEventDestroy(e);
-    if (st->stream) cudaStreamDestroy(st->stream);
+    Kit kit;
+    kit.device = st->device;
+    kit.stream = st->stream;
+    kit.arena = st->arena;
+    kit.d_scalar = st->d_scalar;
+    kit.h_scalar = st->h_scalar;
+    kit.d_err = st->d_err;
+    kit.d_part = st->d_part;
+    kit.part_cap = st->part_cap;
+    kit.d_samp = st->d_samp;
+    kit.samp_cap = st->samp_cap;
+    // a complete kit from a state whose stream finished cleanly goes back to the cache
+    const bool complete = kit.stream && kit.arena.host && kit.arena.dev && kit.d_scalar && kit.h_scalar && kit.d_err;
+    if (!(healthy && complete && give_kit(kit))) free_kit(kit);
     delete st;
 }
 

@@ -250,7 +250,7 @@ def gate_mix_tc(peak_gbs, tf32_tflops=None, qubits=28) -> Dict[str, object]:
 
 
 def serving(peak_gbs, requests=10000, rates=(10000.0, 1000.0, 100.0), low_rate_requests=1000,
-            tvd_samples=24) -> Dict[str, object]:
+            tvd_samples=24, f64_requests=2000) -> Dict[str, object]:
     """The serving stream: Poisson arrivals, qubits log-uniform over 8..26,
     gate-mix circuits of depth U[4, 60], shots log-uniform over 1..8192, 5%
     of requests flagged for f64, seeds from a master seed. Each rate runs
@@ -258,6 +258,9 @@ def serving(peak_gbs, requests=10000, rates=(10000.0, 1000.0, 100.0), low_rate_r
     call; rates whose stream would outlast the others (below 1000 req/s)
     replay the first `low_rate_requests` requests. Programs are compiled
     once and shared by every run (only arrival times depend on the rate).
+    `all_f64`: the first `f64_requests` requests at the highest rate with
+    every request escalated to f64, the form whose every result meets TVD
+    <= 1e-6 against f64.
     Accuracy: f32 requests (up to 22 qubits) run alone at f32 and f64; the
     output distributions' TVD and max |d amp|."""
     from . import serve
@@ -279,6 +282,19 @@ def serving(peak_gbs, requests=10000, rates=(10000.0, 1000.0, 100.0), low_rate_r
         out["rates"].append({"rate_per_s": rate, "requests": count, "server": s, "one_per_call": pl,
                              "throughput_ratio": s["circuits_per_s"] / pl["circuits_per_s"],
                              "p99_ratio": pl["p99_ms"] / s["p99_ms"] if s["p99_ms"] else None})
+    # every request at f64 (double-float, within 1e-12 of exact f64): the
+    # stream with every result at TVD <= 1e-6, on the first f64_requests
+    count = min(requests, f64_requests)
+    srv_reqs = serve.request_stream(count, rate=rates[0], master_seed=2024)
+    pl_reqs = serve.request_stream(count, rate=rates[0], master_seed=2024)
+    for a, b, c in zip(srv_reqs, pl_reqs, base):
+        a.program = b.program = c.program
+        a.precision = b.precision = 64
+    s = serve.serve_stream(srv_reqs)
+    pl = serve.plain_stream(pl_reqs)
+    out["all_f64"] = {"rate_per_s": rates[0], "requests": count, "server": s, "one_per_call": pl,
+                      "throughput_ratio": s["circuits_per_s"] / pl["circuits_per_s"],
+                      "note": "every request escalated to f64: results within 1e-12 of exact f64"}
     acc = []
     for q in base:
         if len(acc) >= tvd_samples:

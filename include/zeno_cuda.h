@@ -89,8 +89,8 @@ int zc_finish(zc_state *st);
  * not). Its scratch is a fixed ~0.9 MiB device array that every GPU loading
  * the library keeps until exit. Limits: <= 30 qubits, <= 16384 shots;
  * larger requests get ZC_ERR_INVALID. Queued ops must be flushed first
- * (zc_finish). The call synchronises the state's stream, so it must not be
- * made on a stream that is being captured. The first call on a device
+ * (zc_finish). The call synchronises the state's stream (it routes the
+ * draws on the host between its two kernels). The first call on a device
  * resolves the array's device address. All calls share the array: calls
  * that overlap (on the GPU or from several threads) race. */
 int zc_sample_noalloc(zc_state *st, uint64_t shots, uint64_t seed, uint64_t *out);

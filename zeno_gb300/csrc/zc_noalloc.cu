@@ -12,9 +12,8 @@
 // file-scope __device__ array of fixed size (kScratchBytes, about 0.9 MiB),
 // which every GPU that loads the library holds until the process exits.
 //
-// The call synchronises the state's stream (it routes the draws on the
-// host between its two kernels), so it must not be made on a stream that
-// is being captured into a CUDA graph.
+// The call synchronises the state's stream: it routes the draws on the
+// host between its two kernels.
 //
 // Limits: states of at most 30 qubits (16384 chunks of 2^16 amplitudes) and
 // at most 16384 shots per call; larger requests are refused.

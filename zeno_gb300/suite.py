@@ -6,6 +6,7 @@
   python -m zeno_gb300.suite serving    # request stream at several arrival rates, server vs one-per-call
   python -m zeno_gb300.suite trajectories  # 4096 noisy 16q trajectories, batched vs per-shot
   python -m zeno_gb300.suite tc         # 28q gate mix fused to k=5..7 blocks on tensor cores vs FP64
+  python -m zeno_gb300.suite gatemix    # 28q gate mix on plain sweeps, f32 and f64 fast (device time)
   python -m zeno_gb300.suite sampler    # sample / prob_one per state size, exact and fast
   python -m zeno_gb300.suite tune       # autotuner tables (fusion width x tile shape), 26 qubits
   python -m zeno_gb300.suite dynamic    # 16q dynamic circuit, 4096 shots: batched trajectories vs per-shot
@@ -177,6 +178,20 @@ def tc(args):
                       "ops": len(prog1.ops), "max_abs_damp_vs_f64": d}), flush=True)
 
 
+def gatemix(args):
+    """The depth-60 gate mix on plain sweeps (fusion 1), f32 and f64 fast:
+    device time per kernel class from the in-library profiler."""
+    from . import workloads as W
+
+    n = args.qubits
+    p = C.mixed_circuit(n, 60, 7).to_program()
+    prog = zb.compile(p, 1)
+    for prec in (32, 64):
+        d = W.device_profile(n, prec, zb.FLAG_FAST, prog, 1, 1, 6800.0)
+        print(json.dumps({"workload": "%dq d60 gate mix, f%d fast sweeps" % (n, prec), "ops": len(prog.ops),
+                          "device_ms": d["device_ms"], "kernels": d["kernels"]}), flush=True)
+
+
 def sampler(args):
     """Sampler and reductions per state size, exact and fast mode: wall time of
     one 1024-shot sample and one prob_one, and the per-kernel device times
@@ -265,8 +280,8 @@ def tune(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("what", choices=["qft", "fusion", "big", "serving", "trajectories", "tc", "sampler", "tune",
-                                       "dynamic"])
+    ap.add_argument("what", choices=["qft", "fusion", "big", "serving", "trajectories", "tc", "gatemix", "sampler",
+                                       "tune", "dynamic"])
     ap.add_argument("--sizes", type=int, nargs="*", default=[16, 20, 22, 26, 28, 30])
     ap.add_argument("--qubits", type=int, default=None)
     ap.add_argument("--requests", type=int, default=1000)
@@ -275,7 +290,7 @@ def main():
     ap.add_argument("--server-only", action="store_true", help="serving: skip the one-circuit-per-call arm")
     a = ap.parse_args()
     if a.qubits is None:
-        a.qubits = {"fusion": 30, "big": 33, "tc": 28, "tune": 26, "dynamic": 16}.get(a.what, 30)
+        a.qubits = {"fusion": 30, "big": 33, "tc": 28, "gatemix": 28, "tune": 26, "dynamic": 16}.get(a.what, 30)
     zb.load()
     globals()[a.what](a)
 

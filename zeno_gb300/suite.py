@@ -54,7 +54,7 @@ def qft(args):
 def fusion(args):
     n = args.qubits
     p = C.matching_circuit(n, 40, 7).to_program()
-    for k in range(1, 6):
+    for k in args.fusions:
         prog = zb.compile(p, k)
         for flags, mode in ((zb.FLAG_FAST, "fast"),):
             t, r = _run(p, prog, 64, flags, 1024, 7)
@@ -288,6 +288,7 @@ def main():
     ap.add_argument("--rates", type=float, nargs="*", default=[100.0, 1000.0, 10000.0])
     ap.add_argument("--n-max", type=int, default=26)
     ap.add_argument("--server-only", action="store_true", help="serving: skip the one-circuit-per-call arm")
+    ap.add_argument("--fusions", type=int, nargs="*", default=[1, 2, 3, 4, 5], help="fusion: widths K to run")
     a = ap.parse_args()
     if a.qubits is None:
         a.qubits = {"fusion": 30, "big": 33, "tc": 28, "gatemix": 28, "tune": 26, "dynamic": 16}.get(a.what, 30)

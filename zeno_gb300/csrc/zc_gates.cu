@@ -294,7 +294,9 @@ int run_kq_df(zc_state *st, const uint32_t *qs, uint32_t k, const void *dev_mat)
         attr_set = true;
     }
     const uint64_t ntiles = (p.groups + G - 1) / G;
-    const int blocks = (int)std::min<uint64_t>(ntiles, (uint64_t)st->num_sms * 3);
+    // 32-41 KiB of shared memory and 32 registers per thread: five CTAs fit an
+    // SM (ncu at 26q, k = 5, with three: 72% issue, 31% warps active)
+    const int blocks = (int)std::min<uint64_t>(ntiles, (uint64_t)st->num_sms * 5);
     k_kq_df<<<blocks, kThreads, smem, st->stream>>>((double *)st->re, (double *)st->im, p,
                                                     (const float4 *)dev_mat);
     ZC_CUDA(cudaGetLastError());

@@ -346,6 +346,113 @@ __device__ __forceinline__ void cscale_df(float2 wr, float2 wi, float2 &ar, floa
     ai = ni;
 }
 
+// ------------------------------------------------------------------
+// Packed double-float arithmetic (f32x2).
+//
+// add / sub / mul / fma .rn.f32x2 apply one IEEE FP32 operation to both
+// halves of a 64-bit register pair. The FP32 datapath does the same number
+// of operations per clock either way, but a packed instruction takes one
+// issue slot and one step of a dependency chain for two of them. The
+// double-float sweeps therefore hold a complex amplitude as
+//   H = (re hi, im hi),  L = (re lo, im lo)
+// and run the real and imaginary halves of a rotation through one
+// instruction stream. Each half sees the operations of the scalar
+// routines above in the same order; where a routine subtracts a product p,
+// the packed one adds q = -p (negation is exact and rounding to nearest is
+// symmetric), so both give the same values (a zero may carry the other
+// sign).
+
+__device__ __forceinline__ unsigned long long pk_bits(float2 v) {
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(v.x), "f"(v.y));
+    return r;
+}
+__device__ __forceinline__ float2 pk_float2(unsigned long long r) {
+    float2 v;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(v.x), "=f"(v.y) : "l"(r));
+    return v;
+}
+__device__ __forceinline__ float2 add2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk_bits(a)), "l"(pk_bits(b)));
+    return pk_float2(d);
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk_bits(a)), "l"(pk_bits(b)));
+    return pk_float2(d);
+}
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) {
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(pk_bits(a)), "l"(pk_bits(b)));
+    return pk_float2(d);
+}
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) {
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(pk_bits(a)), "l"(pk_bits(b)), "l"(pk_bits(c)));
+    return pk_float2(d);
+}
+
+// A real double-float coefficient t as pairs: (t hi, t hi), (t lo, t lo),
+// (-t hi, -t hi).
+struct PkReal {
+    float2 h, l, nh;
+};
+
+// [[1, -t], [t, 1]] on (a, b), unnormalised: per half, a - t b equals
+// df_axpy_u(a, -t, b) and b + t a equals df_axpy_u(b, t, a). Both use the
+// product of +t; q = -(t hi * y hi) serves the error term and the sums.
+__device__ __forceinline__ void pk_rot_u(const PkReal &t, float2 &Ha, float2 &La, float2 &Hb, float2 &Lb) {
+    // a - t b
+    float2 q = mul2(t.nh, Hb);
+    float2 e = fma2(t.h, Hb, q);
+    e = fma2(t.h, Lb, e);
+    e = fma2(t.l, Hb, e);  // t b = -q + e
+    float2 s = add2(Ha, q);
+    float2 bb = sub2(s, Ha);
+    float2 r = add2(sub2(Ha, sub2(s, bb)), sub2(q, bb));
+    const float2 nHa = s, nLa = add2(La, sub2(r, e));
+    // b + t a
+    q = mul2(t.nh, Ha);
+    e = fma2(t.h, Ha, q);
+    e = fma2(t.h, La, e);
+    e = fma2(t.l, Ha, e);  // t a = -q + e
+    s = sub2(Hb, q);
+    bb = sub2(s, Hb);
+    r = sub2(sub2(Hb, sub2(s, bb)), add2(q, bb));
+    Lb = add2(Lb, add2(e, r));
+    Hb = s;
+    Ha = nHa;
+    La = nLa;
+}
+
+// (H, L) <-> the scalar routines' (re, im) double-float pairs.
+__device__ __forceinline__ void pk_split(float2 H, float2 L, float2 &ar, float2 &ai) {
+    ar = make_float2(H.x, L.x);
+    ai = make_float2(H.y, L.y);
+}
+__device__ __forceinline__ void pk_join(float2 ar, float2 ai, float2 &H, float2 &L) {
+    H = make_float2(ar.x, ai.x);
+    L = make_float2(ar.y, ai.y);
+}
+
+// Renormalise both halves (df_norm per half).
+__device__ __forceinline__ void pk_renorm(float2 &H, float2 &L) {
+    const float2 h = add2(H, L);
+    L = sub2(L, sub2(h, H));
+    H = h;
+}
+
+// f64 (re, im) <-> packed pairs; to_f64 renormalises first.
+__device__ __forceinline__ void pk_from_f64(double re, double im, float2 &H, float2 &L) {
+    pk_join(df_from_f64(re), df_from_f64(im), H, L);
+}
+__device__ __forceinline__ void pk_to_f64(float2 H, float2 L, double &re, double &im) {
+    pk_renorm(H, L);
+    re = df_to_f64(make_float2(H.x, L.x));
+    im = df_to_f64(make_float2(H.y, L.y));
+}
+
 // Arithmetic policies: 0 = exact reference trees, 1 = FMA-contracted,
 // 2 = double-float on the FP32 pipe (f64 states only).
 enum : int { AR_EXACT = 0, AR_FMA = 1, AR_DF = 2 };

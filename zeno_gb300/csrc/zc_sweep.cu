@@ -132,11 +132,61 @@ __device__ void apply_perm(T *sr, T *si, const OpHead &op, uint64_t base, uint32
 
 // Per-op coefficients converted once per CTA into the compute representation.
 // U1: the 2x2 matrix; D1: entries 0..3 = d0r d0i d1r d1i. Double-float
-// pairs for A == AR_DF, else values of T.
+// pairs for A == AR_DF, else values of T. Double-float RT: v[0] = t, and
+// v[2..5) its packed pairs (PkReal: t hi, t lo, -t hi, each twice).
 template <typename T, int A>
-struct OpCoef {
+struct alignas(16) OpCoef {
     typename std::conditional<A == AR_DF, float2, T>::type v[8];
 };
+
+// The packed pairs of a double-float rotation's t, read where the rotation
+// runs: hoisted above a group's amplitude loads, the pairs of three
+// rotations (18 registers) spill at the 80-register cap.
+template <typename T, int A>
+__device__ __forceinline__ PkReal rot_pairs(const OpCoef<T, A> &c) {
+    float4 a;
+    float2 b;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(a.x), "=f"(a.y), "=f"(a.z), "=f"(a.w)
+                 : "r"(smem_addr(&c.v[2])));
+    asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(b.x), "=f"(b.y) : "r"(smem_addr(&c.v[4])));
+    return PkReal{make_float2(a.x, a.y), make_float2(a.z, a.w), b};
+}
+
+// Double-float sweeps hold each amplitude as packed pairs: slot v of the
+// re array H = (re hi, im hi), of the im array L = (re lo, im lo). The ops
+// outside register passes (rare there) use the scalar routines on split
+// pairs.
+__device__ __forceinline__ void hl_rot_df(float2 t, float2 &Ha, float2 &La, float2 &Hb, float2 &Lb) {
+    float2 ar, ai, br, bi;
+    pk_split(Ha, La, ar, ai);
+    pk_split(Hb, Lb, br, bi);
+    pair_update_rot_df(t, ar, ai, br, bi);
+    pk_join(ar, ai, Ha, La);
+    pk_join(br, bi, Hb, Lb);
+}
+__device__ __forceinline__ void hl_rdf(const float2 *r, float2 &Ha, float2 &La, float2 &Hb, float2 &Lb) {
+    float2 ar, ai, br, bi;
+    pk_split(Ha, La, ar, ai);
+    pk_split(Hb, Lb, br, bi);
+    pair_update_rdf(r, ar, ai, br, bi);
+    pk_join(ar, ai, Ha, La);
+    pk_join(br, bi, Hb, Lb);
+}
+__device__ __forceinline__ void hl_udf(const MatDF &m, float2 &Ha, float2 &La, float2 &Hb, float2 &Lb) {
+    float2 ar, ai, br, bi;
+    pk_split(Ha, La, ar, ai);
+    pk_split(Hb, Lb, br, bi);
+    pair_update_df(m, ar, ai, br, bi);
+    pk_join(ar, ai, Ha, La);
+    pk_join(br, bi, Hb, Lb);
+}
+__device__ __forceinline__ void hl_cscale_df(float2 wr, float2 wi, float2 &H, float2 &L) {
+    float2 ar, ai;
+    pk_split(H, L, ar, ai);
+    cscale_df(wr, wi, ar, ai);
+    pk_join(ar, ai, H, L);
+}
 
 // The kernel's register group size: f64 states outside FMA mode spill at the
 // 80-register cap with more than two general ops (rotations: three); f32
@@ -181,7 +231,7 @@ __device__ __forceinline__ void group_math(const OpHead *ops, const OpCoef<T, A>
             for (int e = 0; e < E; e++)
                 if (!((e >> g) & 1)) {
                     if constexpr (A == AR_DF)
-                        pair_update_rot_df(t, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                        hl_rot_df(t, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
                     else
                         pair_update_rot<T>(t, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
                 }
@@ -193,7 +243,7 @@ __device__ __forceinline__ void group_math(const OpHead *ops, const OpCoef<T, A>
             for (int e = 0; e < E; e++)
                 if (!((e >> g) & 1)) {
                     if constexpr (A == AR_DF)
-                        pair_update_rdf(r, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                        hl_rdf(r, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
                     else
                         pair_update_real<T>(r, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
                 }
@@ -203,7 +253,7 @@ __device__ __forceinline__ void group_math(const OpHead *ops, const OpCoef<T, A>
             for (int i = 0; i < 8; i++) m.v[i] = coef[o + g].v[i];
 #pragma unroll
             for (int e = 0; e < E; e++)
-                if (!((e >> g) & 1)) pair_update_df(m, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                if (!((e >> g) & 1)) hl_udf(m, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
         } else {
             Mat2<T> m;
 #pragma unroll
@@ -338,7 +388,8 @@ __device__ void apply_u1_group_v2(float *sr, float *si, const OpHead *ops, const
 
 // One pass (see GroupInfo) of a double-float sweep. The descriptor's fields
 // are read from shared memory where they are used, which keeps the 80-register
-// budget for the group's amplitudes.
+// budget for the group's amplitudes. xr / xi hold the packed pairs H / L;
+// the rotations run as f32x2 arithmetic.
 // in_f64 / out_f64: the slots hold f64 on entry / must hold f64 on exit (the
 // sweep's first / last pass does the tile's conversion in registers).
 template <typename T, int A, int G, bool ROT_ONLY, bool HAS_DK, bool HAS_CX>
@@ -376,8 +427,8 @@ __device__ void run_pass(const GroupInfo &gi, float2 *sr, float2 *si, const OpHe
                 for (int g = 0; g < G; g++)
                     if ((e >> g) & 1) w ^= HAS_CX ? gi.pm[g] : gi.gm[g];
                 if (in_f64) {
-                    xr[e] = df_from_f64(reinterpret_cast<const double *>(sr)[w]);
-                    xi[e] = df_from_f64(reinterpret_cast<const double *>(si)[w]);
+                    pk_from_f64(reinterpret_cast<const double *>(sr)[w], reinterpret_cast<const double *>(si)[w],
+                                xr[e], xi[e]);
                 } else {
                     xr[e] = sr[w];
                     xi[e] = si[w];
@@ -395,7 +446,10 @@ __device__ void run_pass(const GroupInfo &gi, float2 *sr, float2 *si, const OpHe
                 for (int g = 0; g < G; g++)
                     if (((e >> g) & 1) && gi.tb[g] != 0xff) j ^= 1u << gi.tb[g];
                 const float4 w = __ldg(dtab + j);
-                cscale_df_u(make_float2(w.x, w.y), make_float2(w.z, w.w), xr[e], xi[e]);
+                float2 ar, ai;  // scalar: the packed form needs eight registers per entry
+                pk_split(xr[e], xi[e], ar, ai);
+                cscale_df_u(make_float2(w.x, w.y), make_float2(w.z, w.w), ar, ai);
+                pk_join(ar, ai, xr[e], xi[e]);
             }
         }
         // the diagonal and the rotations chain unnormalised pairs (every
@@ -405,24 +459,24 @@ __device__ void run_pass(const GroupInfo &gi, float2 *sr, float2 *si, const OpHe
 #pragma unroll
         for (int g = 0; g < G; g++) {
             if (ROT_ONLY || ops[o + g].kind == MOP_RT) {
-                const float2 t = coef[o + g].v[0];
+                const PkReal t = rot_pairs(coef[o + g]);
 #pragma unroll
                 for (int e = 0; e < E; e++)
-                    if (!((e >> g) & 1)) pair_update_rot_df_u(t, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                    if (!((e >> g) & 1)) pk_rot_u(t, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
             } else if (ops[o + g].kind == MOP_R1) {
                 float2 r[4];
 #pragma unroll
                 for (int i = 0; i < 4; i++) r[i] = coef[o + g].v[i];
 #pragma unroll
                 for (int e = 0; e < E; e++)
-                    if (!((e >> g) & 1)) pair_update_rdf(r, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                    if (!((e >> g) & 1)) hl_rdf(r, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
             } else {
                 MatDF m;
 #pragma unroll
                 for (int i = 0; i < 8; i++) m.v[i] = coef[o + g].v[i];
 #pragma unroll
                 for (int e = 0; e < E; e++)
-                    if (!((e >> g) & 1)) pair_update_df(m, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
+                    if (!((e >> g) & 1)) hl_udf(m, xr[e], xi[e], xr[e | (1 << g)], xi[e | (1 << g)]);
             }
         }
         const uint32_t vs = v ^ gi.fmask;
@@ -433,8 +487,7 @@ __device__ void run_pass(const GroupInfo &gi, float2 *sr, float2 *si, const OpHe
             for (int g = 0; g < G; g++)
                 if ((e >> g) & 1) w ^= gi.gm[g];
             if (out_f64) {
-                reinterpret_cast<double *>(sr)[w] = df_to_f64(df_renorm(xr[e]));
-                reinterpret_cast<double *>(si)[w] = df_to_f64(df_renorm(xi[e]));
+                pk_to_f64(xr[e], xi[e], reinterpret_cast<double *>(sr)[w], reinterpret_cast<double *>(si)[w]);
             } else {  // the next pass accepts unnormalised pairs
                 sr[w] = xr[e];
                 si[w] = xi[e];
@@ -526,7 +579,7 @@ __device__ void apply_ops(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *c
                 for (uint32_t p = tid; p < size / 2; p += nt) {
                     const uint32_t v0 = ((p >> b) << (b + 1)) | (p & ((1u << b) - 1)), v1 = v0 | (1u << b);
                     R ar = sr[v0], ai = si[v0], br = sr[v1], bi = si[v1];
-                    if constexpr (A == AR_DF) pair_update_rot_df(t, ar, ai, br, bi);
+                    if constexpr (A == AR_DF) hl_rot_df(t, ar, ai, br, bi);
                     else pair_update_rot<T>(t, ar, ai, br, bi);
                     sr[v0 ^ flip] = ar;
                     si[v0 ^ flip] = ai;
@@ -542,7 +595,7 @@ __device__ void apply_ops(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *c
                 for (int i = 0; i < 4; i++) r[i] = coef[o].v[i];
                 for (uint32_t p = tid; p < size / 2; p += nt) {
                     const uint32_t v0 = ((p >> b) << (b + 1)) | (p & ((1u << b) - 1)), v1 = v0 | (1u << b);
-                    if constexpr (A == AR_DF) pair_update_rdf(r, sr[v0], si[v0], sr[v1], si[v1]);
+                    if constexpr (A == AR_DF) hl_rdf(r, sr[v0], si[v0], sr[v1], si[v1]);
                     else pair_update_real<T>(r, sr[v0], si[v0], sr[v1], si[v1]);
                 }
                 __syncthreads();
@@ -552,7 +605,7 @@ __device__ void apply_ops(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *c
 #pragma unroll
             for (int i = 0; i < 8; i++) m.v[i] = coef[o].v[i];
             auto upd = [&](R &ar, R &ai, R &br, R &bi) {
-                if constexpr (A == AR_DF) pair_update_df(m, ar, ai, br, bi);
+                if constexpr (A == AR_DF) hl_udf(m, ar, ai, br, bi);
                 else pair_update<T, A == AR_EXACT>(m, ar, ai, br, bi);
             };
             for (uint32_t p = tid; p < size / 2; p += nt) {
@@ -564,7 +617,7 @@ __device__ void apply_ops(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *c
             const bool tile_one = outer && ((base >> (op.a & ~kOuterFlag)) & 1);
             auto scl = [&](uint32_t v, R &xr, R &xi) {
                 const bool one = outer ? tile_one : ((v >> op.a) & 1);
-                if constexpr (A == AR_DF) cscale_df(coef[o].v[one ? 2 : 0], coef[o].v[one ? 3 : 1], xr, xi);
+                if constexpr (A == AR_DF) hl_cscale_df(coef[o].v[one ? 2 : 0], coef[o].v[one ? 3 : 1], xr, xi);
                 else cscale<T, A == AR_EXACT>(coef[o].v[one ? 2 : 0], coef[o].v[one ? 3 : 1], xr, xi);
             };
             if constexpr (sizeof(R) == 4) {  // four consecutive elements per 16-byte vector
@@ -615,15 +668,16 @@ __device__ void apply_ops(R *sr, R *si, const OpHead *ops, const OpCoef<T, A> *c
             // W: the table entry (T re, T im; or one float4 of double-float pairs)
             using W = typename std::conditional<A == AR_DF, float4, T>::type;
             auto load_w = [&](uint32_t j, W &wr, W &wi) {
-                if constexpr (A == AR_DF) wr = __ldg(dtab + j);
-                else {
+                if constexpr (A == AR_DF) {
+                    wr = __ldg(dtab + j);
+                } else {
                     const P2 w = __ldg(ptab + j);
                     wr = w.x;
                     wi = w.y;
                 }
             };
             auto scl = [&](const W &wr, const W &wi, R &xr, R &xi) {
-                if constexpr (A == AR_DF) cscale_df(make_float2(wr.x, wr.y), make_float2(wr.z, wr.w), xr, xi);
+                if constexpr (A == AR_DF) hl_cscale_df(make_float2(wr.x, wr.y), make_float2(wr.z, wr.w), xr, xi);
                 else cscale<T, A == AR_EXACT>(wr, wi, xr, xi);
             };
             if constexpr (sizeof(R) == 4) {  // four consecutive elements per 16-byte vector
@@ -730,6 +784,14 @@ __device__ void load_job(SweepSmem<T, A> &c, const MicroOp *gops, int nops, uint
                 else
                     c.coef[tid].v[i] = (T)op.m[i];
             }
+            if constexpr (A == AR_DF) {
+                if (op.kind == MOP_RT) {  // the rotation's packed pairs
+                    const float2 t = c.coef[tid].v[0];
+                    c.coef[tid].v[2] = make_float2(t.x, t.x);
+                    c.coef[tid].v[3] = make_float2(t.y, t.y);
+                    c.coef[tid].v[4] = make_float2(-t.x, -t.x);
+                }
+            }
         }
     }
     if (tid == 0) {
@@ -792,18 +854,29 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
     if (c.fail) return false;
     phase ^= 1;
     if constexpr (A == AR_DF) {
-        // The slots hold f64, or (form & kFormInDf) the normalised pairs the
-        // previous sweep left; on exit f64, or (form & kFormOutDf) normalised
-        // pairs. CX / SWAP move slots whatever they hold.
+        // The slots hold f64, or (form & kFormInDf) the normalised packed
+        // pairs the previous sweep left (re slot H, im slot L); on exit f64,
+        // or (form & kFormOutDf) normalised packed pairs. CX / SWAP move slots
+        // whatever they hold. Each conversion reads both slots of an element
+        // before it writes either.
         double *dr = reinterpret_cast<double *>(sre), *di = reinterpret_cast<double *>(sim);
         float2 *fr = reinterpret_cast<float2 *>(sre), *fi = reinterpret_cast<float2 *>(sim);
         const bool in_df = form & kFormInDf, out_df = form & kFormOutDf;
         const bool fuse_in = c.fuse_in && !in_df, fuse_out = c.fuse_out && !out_df;
+        auto to_pairs = [&](uint32_t v) {
+            float2 H, L;
+            pk_from_f64(dr[v], di[v], H, L);
+            fr[v] = H;
+            fi[v] = L;
+        };
+        auto to_f64 = [&](uint32_t v) {
+            double a, b;
+            pk_to_f64(fr[v], fi[v], a, b);
+            dr[v] = a;
+            di[v] = b;
+        };
         if (c.has_arith && !in_df && !c.fuse_in) {
-            for (uint32_t v = tid; v < size; v += blockDim.x) {
-                fr[v] = df_from_f64(dr[v]);
-                fi[v] = df_from_f64(di[v]);
-            }
+            for (uint32_t v = tid; v < size; v += blockDim.x) to_pairs(v);
             __syncthreads();
         }
         apply_ops<T, A, float2>(fr, fi, c.ops, c.coef, c.nops, base, size, tables, &c.bad, c.jlut, nullptr, c.gi,
@@ -812,22 +885,18 @@ __device__ bool process_tile(SweepSmem<T, A> &c, T *re, T *im, uint64_t t, const
         if (c.has_arith && !fuse_out) {  // register passes leave pairs unnormalised
             for (uint32_t v = tid; v < size; v += blockDim.x) {
                 if (out_df) {
-                    fr[v] = df_renorm(fr[v]);
-                    fi[v] = df_renorm(fi[v]);
+                    float2 H = fr[v], L = fi[v];
+                    pk_renorm(H, L);
+                    fr[v] = H;
+                    fi[v] = L;
                 } else {
-                    dr[v] = df_to_f64(df_renorm(fr[v]));
-                    di[v] = df_to_f64(df_renorm(fi[v]));
+                    to_f64(v);
                 }
             }
         } else if (!c.has_arith && in_df != out_df) {  // permutations only: change the form alone
             for (uint32_t v = tid; v < size; v += blockDim.x) {
-                if (in_df) {
-                    dr[v] = df_to_f64(df_renorm(fr[v]));
-                    di[v] = df_to_f64(df_renorm(fi[v]));
-                } else {
-                    fr[v] = df_from_f64(dr[v]);
-                    fi[v] = df_from_f64(di[v]);
-                }
+                if (in_df) to_f64(v);
+                else to_pairs(v);
             }
         }
     } else {
@@ -998,18 +1067,20 @@ int run_sweep_multi(cudaStream_t stream, int num_sms, const char *dev_blob, int 
     return ZC_OK;
 }
 
-// Round a state that double-float sweeps left as (hi, lo) pairs back to f64
-// (the last sweep of a flush normally does this itself; this pass serves a
-// flush whose double-float sweeps are followed by another kernel).
+// Round a state that double-float sweeps left as packed pairs (re slot
+// H = (re hi, im hi), im slot L = (re lo, im lo)) back to f64 (the last sweep
+// of a flush normally does this itself; this pass serves a flush whose
+// double-float sweeps are followed by another kernel).
 __global__ void __launch_bounds__(256) k_df_to_f64(double *__restrict__ re, double *__restrict__ im, uint64_t len) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len; i += (uint64_t)gridDim.x * blockDim.x) {
         const double2 a = reinterpret_cast<const double2 *>(re)[i];
         const double2 b = reinterpret_cast<const double2 *>(im)[i];
         const float4 fa = *reinterpret_cast<const float4 *>(&a), fb = *reinterpret_cast<const float4 *>(&b);
-        reinterpret_cast<double2 *>(re)[i] = make_double2(df_to_f64(df_renorm(make_float2(fa.x, fa.y))),
-                                                          df_to_f64(df_renorm(make_float2(fa.z, fa.w))));
-        reinterpret_cast<double2 *>(im)[i] = make_double2(df_to_f64(df_renorm(make_float2(fb.x, fb.y))),
-                                                          df_to_f64(df_renorm(make_float2(fb.z, fb.w))));
+        double r0, i0, r1, i1;
+        pk_to_f64(make_float2(fa.x, fa.y), make_float2(fb.x, fb.y), r0, i0);
+        pk_to_f64(make_float2(fa.z, fa.w), make_float2(fb.z, fb.w), r1, i1);
+        reinterpret_cast<double2 *>(re)[i] = make_double2(r0, r1);
+        reinterpret_cast<double2 *>(im)[i] = make_double2(i0, i1);
     }
 }
 

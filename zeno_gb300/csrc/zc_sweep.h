@@ -14,8 +14,9 @@ enum : uint32_t { MOP_U1 = 1, MOP_D1 = 2, MOP_DK = 3, MOP_CX = 4, MOP_SWAP = 5, 
 
 // Tile geometry: local qubits are 0..L-1 plus hpos[0..H) (ascending).
 // form (double-float sweeps of f64 states): kFormInDf — the state holds
-// (hi, lo) float pairs on entry (the previous sweep left them); kFormOutDf —
-// leave normalised pairs for the next sweep instead of rounding to f64.
+// packed float pairs on entry (the previous sweep left them: re slot
+// (re hi, im hi), im slot (re lo, im lo)); kFormOutDf — leave normalised
+// pairs for the next sweep instead of rounding to f64.
 constexpr uint32_t kFormInDf = 1u, kFormOutDf = 2u;
 struct SweepGeom {
     uint32_t n, L, H, form;

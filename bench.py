@@ -39,12 +39,17 @@ METRIC = "30q circuit throughput (u3 + matching-CX, depth 40, f64)"
 # DRAM read+write per launch over algorithmic bytes, from an ncu capture of
 # the f64 double-float sweep kernel at 26 qubits (state 8x the L2; the sweeps
 # between the first and the last of a flush, which hand the state over as
-# double-float pairs): 1.074 GB read + 1.025 GB write against 2S = 2.147 GB.
-MEASURED_TRAFFIC_RATIO = {"sweep": (1.074e9 + 1.025e9) / 2.147e9}
-# The same capture: issue slots 58-61% busy, FMA pipe 41-42%, ALU pipe 22-23%, FP64 0%.
-SWEEP_DF_PIPES = {"issue_active_pct": 58.2, "fma_pipe_pct": 40.9, "alu_pipe_pct": 21.9, "fp64_pipe_pct": 0.0}
-# FP32 instructions per amplitude of each double-float sweep micro-op
-# (zeno_gb300/csrc/zc_arith.cuh): a product is 4 (FMUL + 3 FFMA), TwoSum 6,
+# packed double-float pairs): 1.074 GB read + 1.029 GB write against
+# 2S = 2.147 GB.
+MEASURED_TRAFFIC_RATIO = {"sweep": (1.074e9 + 1.029e9) / 2.147e9}
+# The same capture: issue slots 50-51% busy, FMA pipe 30-31% of its
+# instruction peak and 46% of its cycles (packed f32x2 rotations), ALU pipe
+# 24-25%, FP64 0%.
+SWEEP_DF_PIPES = {"issue_active_pct": 49.6, "fma_pipe_pct": 30.0, "fma_pipe_cycles_pct": 46.2, "alu_pipe_pct": 24.3,
+                  "fp64_pipe_pct": 0.0}
+# FP32 operations per amplitude of each double-float sweep micro-op
+# (zeno_gb300/csrc/zc_arith.cuh; rotations issue them as packed f32x2
+# instructions, two operations each): a product is 4 (MUL + 3 FMA), TwoSum 6,
 # renormalisation 3. Complex 2x2: four 4-term dot products per pair
 # (4*4 + 3*6 + 6 + 3 = 43 each) = 86; real 2x2 and one-qubit diagonals:
 # 2-term dot products (2*4 + 6 + 2 + 3 = 19), two per amplitude = 38. Register
@@ -52,7 +57,7 @@ SWEEP_DF_PIPES = {"issue_active_pct": 58.2, "fma_pipe_pct": 40.9, "alu_pipe_pct"
 # rotation [[1, -t], [t, 1]] 2 x (4 + 6 + 2) = 24 (one renormalisation per
 # sweep, where the tile goes back to f64, is not counted). CX and SWAP move
 # data only.
-DF_FP32_INSTR_PER_AMP = {"complex": 86, "diag1": 38, "diag_table": 32, "cx": 0, "swap": 0, "real": 38,
+DF_FP32_OPS_PER_AMP = {"complex": 86, "diag1": 38, "diag_table": 32, "cx": 0, "swap": 0, "real": 38,
                          "rotation": 24}
 CONFIG_NAMES = ("matching_20q", "qft", "fusion_sweep", "big_state", "trajectories", "gate_mix_tc", "serving")
 
@@ -457,7 +462,7 @@ def main():
     value, elapsed = job_throughput(a.steps, elapsed, ws)
     gates_ms = sum(d["ms"] for d in classes.values())  # all of our kernels in the timed region
     mops = {k: c1["micro_ops"][k] - c0["micro_ops"][k] for k in c1["micro_ops"]}
-    fp32_instr = sum(n * DF_FP32_INSTR_PER_AMP[k] for k, n in mops.items()) * float(1 << a.qubits)
+    fp32_ops = sum(n * DF_FP32_OPS_PER_AMP[k] for k, n in mops.items()) * float(1 << a.qubits)
     dom = max(classes, key=lambda c: classes[c]["ms"])
     dd = classes[dom]
     achieved = (dd["bytes"] / dd["launches"]) / (dd["ms"] / dd["launches"] / 1000.0) / 1e9
@@ -487,17 +492,19 @@ def main():
                      "traffic": (MEASURED_TRAFFIC_RATIO[dom] * dd["bytes"] / dd["launches"]
                                  if dom in MEASURED_TRAFFIC_RATIO else None),
                      "ops_per_launch": len(ops) * a.steps / dd["launches"] if dom == "sweep" else 1.0,
-                     "limiter": ("FP32/ALU issue: each sweep applies many gates per HBM pass in double-float "
-                                 "arithmetic; ncu at 26q: %s" % SWEEP_DF_PIPES) if df_sweep else None,
-                     "compute": ({"bound": "fp32_pipe", "unit": "FP32 instr/s",
-                                  "achieved": fp32_instr / (dd["ms"] / 1e3),
+                     "limiter": ("double-float arithmetic on the FP32 pipe, not HBM: each sweep applies many "
+                                 "gates per HBM pass; the rest is barrier and L1 latency; ncu at 26q: %s"
+                                 % SWEEP_DF_PIPES) if df_sweep else None,
+                     "compute": ({"bound": "fp32_pipe", "unit": "FP32 op/s",
+                                  "achieved": fp32_ops / (dd["ms"] / 1e3),
                                   "peak": pk["fp32_fma_per_s"], "peak_source": "measured live (zc_measure_arith_peaks)",
-                                  "frac": fp32_instr / (dd["ms"] / 1e3) / pk["fp32_fma_per_s"],
+                                  "frac": fp32_ops / (dd["ms"] / 1e3) / pk["fp32_fma_per_s"],
                                   "micro_ops": mops,
-                                  "count": "sweep micro-ops issued in the timed steps x FP32 instructions per "
-                                           "amplitude of their double-float arithmetic %s; index arithmetic, "
-                                           "data moves and f64 <-> double-float conversions not counted"
-                                           % DF_FP32_INSTR_PER_AMP}) if df_sweep else None},
+                                  "count": "sweep micro-ops issued in the timed steps x FP32 operations per "
+                                           "amplitude of their double-float arithmetic %s (a packed f32x2 "
+                                           "instruction is two); index arithmetic, data moves and f64 <-> "
+                                           "double-float conversions not counted" % DF_FP32_OPS_PER_AMP})
+                     if df_sweep else None},
         "peaks": pk,
         "clocks": clk.summary(),
     }

@@ -171,12 +171,20 @@ def test_config_shape_matches_per_shot_oracle(zc, oracle):
     g = _bits(batched(zc, p, ng, 21, noise).counts, n)
     o = _bits(oracle.run(p, prec=32, shots=no, seed=22, noise=noise)[0], n)
     assert g.shape == (ng, n) and o.shape == (no, n)
+    _agree(g, o, n)
+
+
+def _agree(g, o, n):
+    """Shots of the batched engine (g) and of the per-shot oracle (o) agree:
+    every qubit's P(1) at 6 sigma, and each block of four qubits' 16-outcome
+    distribution by TVD within 6 sigma of the TVD sampling alone gives."""
+    ng, no = len(g), len(o)
     pg, po = g.mean(axis=0), o.mean(axis=0)
     for q in range(n):
         sig = math.sqrt(max(pg[q] * (1 - pg[q]), 1e-12) * (1.0 / ng + 1.0 / no))
         assert abs(pg[q] - po[q]) <= 6 * sig, (q, pg[q], po[q], sig)
     w = 1 << np.arange(4)
-    for b0 in range(0, n, 4):
+    for b0 in range(0, n - 3, 4):
         hg = np.bincount(g[:, b0:b0 + 4] @ w, minlength=16) / ng
         ho = np.bincount(o[:, b0:b0 + 4] @ w, minlength=16) / no
         d = 0.5 * np.abs(hg - ho).sum()
@@ -184,3 +192,18 @@ def test_config_shape_matches_per_shot_oracle(zc, oracle):
         mean = 0.5 * np.sum(np.sqrt(2 / np.pi * var))  # E|N(0, var)| = sqrt(2 var / pi)
         std = 0.5 * np.sqrt(np.sum((1 - 2 / np.pi) * var))
         assert d <= mean + 6 * std, (b0, d, mean, std)
+
+
+@pytest.mark.parametrize("n", (13, 14, 15))
+def test_noisy_13_to_15_qubits_match_per_shot_oracle(zc, oracle, n):
+    """Noisy circuits of 13-15 qubits, with noise strong enough that
+    depolarizing, both flips and damping all fire, against the oracle's
+    per-shot replay: per-qubit marginals and four-qubit blocks."""
+    noise = zc.NoiseModel(depolarizing_1q=0.01, depolarizing_2q=0.03, amplitude_damping=0.02, bit_flip=0.005,
+                          phase_flip=0.01, readout_flip_0to1=0.02, readout_flip_1to0=0.02)
+    p = C.matching_circuit(n, 4, 40 + n).to_program()
+    ng, no = 1 << 16, 2048
+    g = _bits(batched(zc, p, ng, 31, noise).counts, n)
+    o = _bits(oracle.run(p, prec=32, shots=no, seed=32, noise=noise)[0], n)
+    assert g.shape == (ng, n) and o.shape == (no, n)
+    _agree(g, o, n)

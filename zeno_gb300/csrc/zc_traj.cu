@@ -256,7 +256,10 @@ __global__ void __launch_bounds__(kTrajThreads, 4)
                 }
             }
             __syncthreads();
-            if (s.skip) continue;  // pending operators wait for the next op that runs
+            if (s.skip) {  // pending operators wait for the next op that runs
+                __syncthreads();  // every thread has read s.skip before thread 0 sets it again
+                continue;
+            }
             if (tid == 0) {
                 prepare_pending(s);
                 const double pdep = gate ? (k == 1 ? nz.p[0] : nz.p[1]) : 0.0;

@@ -266,3 +266,60 @@ def test_qft_22q_exact_and_fast(zc, oracle):
     dim = 1 << 22
     want = np.exp(2j * np.pi * x * np.arange(dim) / dim) / np.sqrt(dim)
     assert np.abs(sv - want).max() < 1e-11 and np.abs(fa.statevector - want).max() < 1e-11
+
+
+def _apply(g, o, op):
+    if op[0] == "u":
+        g.apply_unitary(op[1], op[2])
+        o.apply_unitary(op[1], op[2])
+    elif op[0] == "d":
+        g.apply_diagonal(op[1], op[2])
+        o.apply_diagonal(op[1], op[2])
+    elif op[0] == "cx":
+        g.apply_cx(op[1], op[2])
+        o.apply_cx(op[1], op[2])
+    else:
+        swap = np.zeros((4, 4), complex)
+        for c in range(4):
+            swap[((c & 1) << 1) | ((c >> 1) & 1), c] = 1
+        g.apply_swap(op[1], op[2])
+        o.apply_unitary(sorted(op[1:3]), swap)
+
+
+@pytest.mark.parametrize("n", (16, 19))
+def test_fast_f64_sweeps_blocks_and_reads_interleaved(zc, oracle, n):
+    """Fast f64 across the boundaries of its sweeps: runs of sweeps hand the
+    state over as packed double-float pairs, and a dense 2- or 3-qubit block
+    or a read (prob_one, measure, norm) in the middle of the program first
+    turns it back into f64. Every read and the final state stay within 1e-12
+    of the FP64 oracle."""
+    rng = np.random.default_rng(n)
+    amps = rand_state(n, 70 + n, normalize=True)
+    ops = random_ops(n, 240, 90 + n)
+    ops = [("u", op[1], np.linalg.qr(op[2])[0]) if op[0] == "u" else op for op in ops]
+    ops = [("d", op[1], op[2] / np.abs(op[2])) if op[0] == "d" else op for op in ops]
+    g = zc.CudaBackend(n, 64, zc.FLAG_FAST)
+    o = oracle.State(n, 64)
+    g.load_state(amps)
+    o.load(amps)
+    reads = 0
+    for i, op in enumerate(ops):
+        _apply(g, o, op)
+        if i % 60 == 30:  # a three-qubit dense block between sweeps
+            qs = sorted(int(x) for x in rng.choice(n, 3, replace=False))
+            _apply(g, o, ("u", qs, np.linalg.qr(rand_matrix(8, 5000 + i))[0]))
+        if i % 40 == 39:
+            q = int(rng.integers(0, n))
+            p = o.prob_one(q)
+            assert abs(g.prob_one(q) - p) <= 1e-12, (i, q)
+            if i % 80 == 79:
+                u = 0.5 if abs(p - 0.5) > 1e-6 else 0.25
+                assert g.measure(q, u) == o.measure(q, u), (i, q)
+            assert abs(g.norm_sqr() - o.norm_sqr()) <= 1e-12, i
+            reads += 1
+    assert reads == 6
+    d = np.abs(g.statevector() - o.statevector()).max()
+    assert d < 1e-12, d
+    c = g.counters()
+    assert c["sweeps"] > 0
+    g.close()

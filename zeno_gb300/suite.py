@@ -37,12 +37,14 @@ def _run(p, prog, prec, flags, shots, seed):
 
 
 def qft(args):
-    for n in (24, 28):
+    for n in ((args.qubits,) if args.qubits else (24, 28)):
         c, x = C.qft_circuit(n, 11)
         p = c.to_program()
         prog = zb.compile(p, 1)
-        for prec in (64, 32):
+        for prec in args.precisions:
             for flags, mode in ((zb.FLAG_EXACT, "exact"), (zb.FLAG_FAST, "fast")):
+                if mode not in args.modes:
+                    continue
                 _run(p, prog, prec, flags, 8192, 3)
                 t, r = _run(p, prog, prec, flags, 8192, 3)
                 print(json.dumps({"workload": "qft", "qubits": n, "precision": prec, "mode": mode, "seconds": t,
@@ -289,6 +291,9 @@ def main():
     ap.add_argument("--n-max", type=int, default=26)
     ap.add_argument("--server-only", action="store_true", help="serving: skip the one-circuit-per-call arm")
     ap.add_argument("--fusions", type=int, nargs="*", default=[1, 2, 3, 4, 5], help="fusion: widths K to run")
+    ap.add_argument("--precisions", type=int, nargs="*", default=[64, 32], help="qft: state precisions to run")
+    ap.add_argument("--modes", nargs="*", default=["exact", "fast"], choices=["exact", "fast"],
+                    help="qft: arithmetic modes to run")
     a = ap.parse_args()
     if a.qubits is None:
         a.qubits = {"fusion": 30, "big": 33, "tc": 28, "gatemix": 28, "tune": 26, "dynamic": 16}.get(a.what, 30)

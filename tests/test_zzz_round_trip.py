@@ -72,3 +72,25 @@ def test_headline_circuit_round_trip_30q(zc):
     assert abs(norm - 1.0) < 1e-9, norm
     assert p1 < 1e-12, p1
     assert not np.any(idx), np.unique(idx)[:8]
+
+
+@pytest.mark.gpu
+def test_headline_circuit_fast_vs_exact_30q(zc):
+    """The headline circuit itself at its full size: fast f64 against exact
+    mode, which reproduces zeno's arithmetic bit for bit (the oracle
+    comparisons at every size the oracle can hold). max |d amp| within the
+    fast-mode 1e-12 and TVD <= 1e-6, compared in chunks of the two 16 GiB
+    states."""
+    n = 30
+    p = C.matching_circuit(n, 40, 7, measure=False).to_program()
+    prog = zc.compile(p, 1)
+    fast = zc.run(p, shots=0, precision=64, statevector=True, flags=zc.FLAG_FAST, program=prog).statevector
+    exact = zc.run(p, shots=0, precision=64, statevector=True, flags=zc.FLAG_EXACT, program=prog).statevector
+    assert fast.shape == exact.shape == (1 << n,)
+    d, tvd, chunk = 0.0, 0.0, 1 << 24
+    for i in range(0, 1 << n, chunk):
+        a, b = fast[i:i + chunk], exact[i:i + chunk]
+        d = max(d, float(np.abs(a - b).max()))
+        tvd += 0.5 * float(np.abs(np.abs(a) ** 2 - np.abs(b) ** 2).sum())
+    assert d < 1e-12, d
+    assert tvd < 1e-6, tvd

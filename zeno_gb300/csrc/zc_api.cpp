@@ -460,7 +460,7 @@ static bool sweepable(const QOp &op);
 static bool sweeps_enabled(const zc_state *st);
 
 // Before any kernel other than a sweep: a state that double-float sweeps
-// left as (hi, lo) pairs goes back to f64.
+// left as packed float pairs goes back to f64.
 static int settle_form(zc_state *st) {
     if (!st->df_resident) return ZC_OK;
     st->df_resident = false;

@@ -86,7 +86,7 @@ struct zc_state {
     void *d_samp = nullptr;      // sampler work area
     size_t samp_cap = 0;
     int *d_err = nullptr;        // device error flag (sweep wait timeouts)
-    bool df_resident = false;    // inside a flush: fast f64 sweeps left (hi, lo) float pairs in re / im
+    bool df_resident = false;    // inside a flush: fast f64 sweeps left packed float pairs in re / im
     std::vector<zc::QOp> queue;  // ops waiting to be scheduled into sweeps
     bool prof = false;            // record CUDA events around every launch
     std::vector<zc::ProfRec> prof_recs;

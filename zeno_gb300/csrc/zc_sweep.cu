@@ -7,9 +7,10 @@
 // fetched with one TMA bulk copy (cp.async.bulk, completion on an
 // mbarrier), the sweep's micro-ops are applied in shared memory, and the
 // rows go back with TMA bulk stores; three CTAs per SM overlap one tile's
-// copies with the others' arithmetic. Every micro-op uses the same
-// arithmetic as the per-op kernels, so a sweep is bit-identical to
-// launching its ops one by one.
+// copies with the others' arithmetic. In exact mode every micro-op uses the
+// same arithmetic as the per-op kernels, so a sweep is bit-identical to
+// launching its ops one by one; fast f64 sweeps run the lowered ops
+// (zc_lower.cpp) in register passes of packed double-float arithmetic.
 //
 // Which ops fit a sweep: unitaries whose qubits are all local; diagonals
 // on any qubits (bits of non-local qubits are constant per tile); CX with a

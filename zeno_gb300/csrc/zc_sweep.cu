@@ -156,8 +156,7 @@ __device__ __forceinline__ PkReal rot_pairs(const OpCoef<T, A> &c) {
 
 // Double-float sweeps hold each amplitude as packed pairs: slot v of the
 // re array H = (re hi, im hi), of the im array L = (re lo, im lo). The ops
-// outside register passes (rare there) use the scalar routines on split
-// pairs.
+// outside register passes use the scalar routines on split pairs.
 __device__ __forceinline__ void hl_rot_df(float2 t, float2 &Ha, float2 &La, float2 &Hb, float2 &Lb) {
     float2 ar, ai, br, bi;
     pk_split(Ha, La, ar, ai);
@@ -182,10 +181,12 @@ __device__ __forceinline__ void hl_udf(const MatDF &m, float2 &Ha, float2 &La, f
     pk_join(ar, ai, Ha, La);
     pk_join(br, bi, Hb, Lb);
 }
+// Diagonal factors leave the pairs unnormalised, as in register passes: the
+// ops after them accept that, and the sweep's exit renormalises.
 __device__ __forceinline__ void hl_cscale_df(float2 wr, float2 wi, float2 &H, float2 &L) {
     float2 ar, ai;
     pk_split(H, L, ar, ai);
-    cscale_df(wr, wi, ar, ai);
+    cscale_df_u(wr, wi, ar, ai);
     pk_join(ar, ai, H, L);
 }
 

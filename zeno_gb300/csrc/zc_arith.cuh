@@ -280,18 +280,6 @@ __device__ __forceinline__ float2 df_dot2_u(float2 x0, float2 y0, float2 x1, flo
 
 __device__ __forceinline__ float2 df_renorm(float2 v) { return df_norm(v.x, v.y); }
 
-__device__ __forceinline__ void pair_update_rot_df_u(float2 t, float2 &ar, float2 &ai, float2 &br, float2 &bi) {
-    const float2 nt = df_neg(t);
-    const float2 nar = df_axpy_u(ar, nt, br);
-    const float2 nai = df_axpy_u(ai, nt, bi);
-    const float2 nbr = df_axpy_u(br, t, ar);
-    const float2 nbi = df_axpy_u(bi, t, ai);
-    ar = nar;
-    ai = nai;
-    br = nbr;
-    bi = nbi;
-}
-
 __device__ __forceinline__ void cscale_df_u(float2 wr, float2 wi, float2 &ar, float2 &ai) {
     const float2 nr = df_dot2_u(wr, ar, df_neg(wi), ai);
     const float2 ni = df_dot2_u(wr, ai, wi, ar);
